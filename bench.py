@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark: LOD0 decode throughput of the 1024^3 synthetic scroll volume
+encoded at target_ratio 10 (the per-atom codec path's headline workload).
+
+GPU arm (default): the archive is produced by this library's vc_encode on the
+device, opened and made resident; one step = vcg_decode_lod_device(LOD0) with
+the archive and the 1 GiB output in HBM (L2 flushed between steps by a 512 MiB
+write). `e2e` = one step through the drop-in C ABI with host buffers:
+vc_open on a pinned host archive + vc_decode_lod into pinned host memory +
+vc_close (archive upload, atom-table build, decode and copy-out all timed).
+
+Reference arm (--impl reference): the reference's CPU decode of the same LOD0
+(oracle/_ref when the reference was built on this host, else the C oracle
+port), a parallel-for over atoms on all host cores.
+
+Multi-GPU: replicas (each rank decodes its own copy; no data-path collective).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "volume-compressor_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "LOD0 decode/encode GB/s; region p50/p99 µs; bit-exact vs reference"
+CONFIG_ID = 2
+
+
+def args_parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--size", type=int, default=1024)
+    p.add_argument("--target", type=float, default=10.0)
+    p.add_argument("--regions", type=int, default=200)
+    return p.parse_args()
+
+
+def golden_case(size, target):
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            cases = {c["name"]: c for c in json.load(f)["cases"]}
+        return cases.get(f"cfg2_{size}_t{int(target)}")
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------- distributed plumbing
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        os.environ.setdefault("VC_DEVICE", str(self.local))
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)])
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)])
+        self.pg.all_reduce(t)
+        return float(t.item())
+
+
+# ---------------------------------------------------------------- clocks
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-i", str(gpu_index), "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle / reference)
+def cpu_decode_setup(size, target, threads):
+    """Archive of the benchmark volume built on the CPU with the oracle at the
+    reference's q (from the golden fixture), for the CPU arms."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oraclelib
+    import vc_gb300 as vc
+    g = golden_case(size, target)
+    vol = vc.synth(size, size, size, vc.config_seed(CONFIG_ID), threads=threads)
+    if g:
+        q0 = g["q0"]
+    else:
+        q0, _, _ = oraclelib.rate_control(vol, target, threads)
+    import numpy as np
+    qs, q = [], np.float32(q0)
+    for _ in range(8):
+        qs.append(float(max(q, np.float32(0.05))))
+        q = np.float32(q * np.float32(0.6))
+    s, data = oraclelib.encode_fixed_q(vol, target, qs, threads)
+    assert s == 0
+    return data, q0
+
+
+def cpu_decoder(data, threads):
+    """Returns (kind, decode_fn) timing a full LOD0 decode on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    ref_so = os.path.join(ROOT, "oracle", "_ref", "libvcref.so")
+    if os.path.exists(ref_so):
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+            import refcodec
+            from concurrent.futures import ThreadPoolExecutor
+            a = refcodec.RefArchive(data)
+            _, (nx, ny, nz) = a.lod_dims(0)
+            atoms = [(ax, ay, az) for az in range((nz + 31) // 32) for ay in range((ny + 31) // 32)
+                     for ax in range((nx + 31) // 32)]
+            L = refcodec.lib()
+            bufs = [np.zeros(32768, np.uint8) for _ in range(threads)]
+            out = np.zeros((nz, ny, nx), np.uint8)
+
+            def chunk(k):
+                b = bufs[k]
+                for (ax, ay, az) in atoms[k::threads]:
+                    L.vc_decode_atom(a.h, 0, ax, ay, az, b.ctypes.data)
+                    v = b.reshape(32, 32, 32)
+                    z1, y1, x1 = min(32, nz - az * 32), min(32, ny - ay * 32), min(32, nx - ax * 32)
+                    out[az * 32:az * 32 + z1, ay * 32:ay * 32 + y1, ax * 32:ax * 32 + x1] = v[:z1, :y1, :x1]
+
+            def run():
+                with ThreadPoolExecutor(threads) as ex:
+                    list(ex.map(chunk, range(threads)))
+                return out
+            return "reference", run
+        except OSError:
+            pass
+    import oraclelib
+    a = oraclelib.Archive(data)
+
+    def run():
+        s, out = a.decode_lod(0, threads=threads)
+        assert s == 0
+        return out
+    return "port", run
+
+
+# ---------------------------------------------------------------- arms
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    data, q0 = cpu_decode_setup(args.size, args.target, threads)
+    kind, run = cpu_decoder(data, threads)
+    for _ in range(args.warmup):
+        run()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run()
+    dt = time.perf_counter() - t0
+    nbytes = args.size ** 3
+    gbps = args.steps * nbytes / dt / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": gbps, "unit": "GB/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "i32",
+            "data": "synthetic",
+            "config": {"workload": f"LOD0 decode, {args.size}^3 u8 synthetic scroll volume, target_ratio "
+                                   f"{args.target:g}", "q0": q0, "archive_bytes": len(data)},
+            "cpu_baseline": {"value": gbps, "unit": "GB/s", "cores": threads, "kind": kind,
+                             "sample": f"full LOD0 decode ({nbytes} voxels) per step, parallel-for over atoms"},
+            "e2e": {"value": gbps, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def gb300_arm(args, dist):
+    import numpy as np
+    import vc_gb300 as vc
+    if not os.path.exists(vc.LIB_PATH):
+        vc.build()
+    n = args.size
+    nbytes = n ** 3
+    dims = (n, n, n)
+    s, nsm, cc = vc.device_info()
+    assert s == 0, vc.last_error()
+    g = golden_case(n, args.target)
+
+    # workload: synthetic volume on the device, encoded by this library
+    dvol = vc.synth_device(n, n, n, vc.config_seed(CONFIG_ID))
+    s, data, q0 = vc.encode_device(dvol, dims, args.target)
+    assert s == 0, vc.last_error()
+    enc_full_ms = vc.last_call_ms()
+    qs, q = [], np.float32(q0)
+    for _ in range(8):
+        qs.append(float(max(q, np.float32(0.05))))
+        q = np.float32(q * np.float32(0.6))
+    enc_ms = []
+    for _ in range(2):
+        s, data_q = vc.encode_q(dvol, args.target, qs, on_device=dims)
+        assert s == 0 and data_q == data
+        enc_ms.append(vc.last_call_ms())
+    bit_exact_archive = (g["sha256"] == __import__("hashlib").sha256(data).hexdigest()) if g else None
+
+    arc = vc.Archive(data)
+    assert arc.make_resident() == 0
+    out = vc.DeviceBuffer(nbytes)
+    flush = vc.DeviceBuffer(512 << 20)
+    for _ in range(args.warmup):
+        assert arc.decode_lod_device(0, out) == 0
+    lod0_ok = None
+    if g:
+        import hashlib
+        lod0_ok = hashlib.sha256(out.download(nbytes).tobytes()).hexdigest() == g["lod_sha256"][0]
+
+    vc.profile_enable(True)
+    vc.profile_read(reset=True)
+    dist.barrier()
+    vc.sync()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    ms = []
+    for k in range(args.steps):
+        vc.lib().vcg_memset(flush.ptr, k & 0xFF, flush.nbytes)   # L2 flush, not timed
+        assert arc.decode_lod_device(0, out) == 0
+        ms.append(vc.last_call_ms())
+    vc.sync()
+    clk = clocks.stop()
+    dist.barrier()
+    stats = vc.profile_read(reset=True)
+    vc.profile_enable(False)
+    total_ms = dist.max(sum(ms))
+    value = dist.sum(args.steps * nbytes) / (total_ms / 1e3) / 1e9
+
+    # e2e through the drop-in ABI with pinned host buffers
+    L = vc.lib()
+    hp = L.vcg_alloc_host(len(data))
+    ctypes.memmove(hp, data, len(data))
+    ho = L.vcg_alloc_host(nbytes)
+    d = vc.Dims()
+    e2e_t = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        h = L.vc_open(hp, len(data))
+        st = L.vc_decode_lod(h, 0, ho, ctypes.byref(d))
+        L.vc_close(h)
+        t1 = time.perf_counter()
+        assert st == 0
+        if k >= args.warmup:
+            e2e_t.append(t1 - t0)
+    e2e_s = dist.max(sum(e2e_t))
+    e2e = dist.sum(args.steps * nbytes) / e2e_s / 1e9
+    L.vcg_free_host(hp)
+    L.vcg_free_host(ho)
+
+    # per-request region latency (plain path, host output)
+    rng = np.random.default_rng(0xB0C5)
+    lat = []
+    for _ in range(args.regions):
+        lod = int(rng.integers(0, 4))
+        dd = arc.lod_dims(lod)[1]
+        e = [int(min(rng.integers(32, 257), dd[k])) for k in range(3)]
+        o = [int(rng.integers(0, dd[k] - e[k] + 1)) for k in range(3)]
+        box = (o[0], o[1], o[2], o[0] + e[0], o[1] + e[1], o[2] + e[2])
+        t0 = time.perf_counter()
+        st, _ = arc.decode_region(lod, box)
+        lat.append((time.perf_counter() - t0) * 1e6)
+        assert st == 0
+    lat.sort()
+
+    # roofline of the dominant stage
+    peak, peak_kind = measured_peak()
+    dom = max((k for k in stats if k in ("idct", "rc_decode")), key=lambda k: stats[k]["ms"])
+    st_ = stats[dom]
+    per_launch_bytes = (st_["bytes_read"] + st_["bytes_written"]) / max(1, st_["launches"])
+    per_launch_ms = st_["ms"] / max(1, st_["launches"])
+    achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+    launches = int(sum(v["launches"] for v in stats.values()))
+
+    cpu = None
+    if dist.rank == 0 and os.environ.get("VC_BENCH_NO_CPU") != "1":
+        threads = os.cpu_count() or 1
+        kind, run = cpu_decoder(data, threads)
+        t0 = time.perf_counter()
+        ref_out = run()
+        dt = time.perf_counter() - t0
+        cpu = {"value": nbytes / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": kind,
+               "sample": f"one full LOD0 decode ({nbytes} voxels) of the same archive, parallel-for over atoms"}
+        if lod0_ok is None:
+            lod0_ok = bool(np.array_equal(out.download(nbytes), ref_out.ravel()))
+
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "i32", "data": "synthetic",
+        "config": {"workload": f"LOD0 decode, {n}^3 u8 synthetic scroll volume (seed 0x5EED0002), "
+                               f"target_ratio {args.target:g}, archive resident in HBM",
+                   "volume": list(dims), "target_ratio": args.target, "q0": q0, "archive_bytes": len(data),
+                   "l2": "flushed between timed steps (512 MiB device write)", "parallelism": f"replicas{dist.world}"},
+        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": nbytes},
+        "gpu_launches": launches,
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
+        "stages": {k: {"ms_per_step": v["ms"] / args.steps, "GBps_algorithmic":
+                       (v["bytes_read"] + v["bytes_written"]) / max(1e-9, v["ms"] / 1e3) / 1e9}
+                   for k, v in stats.items()},
+        "encode_GBps": nbytes / (statistics.median(enc_ms) / 1e3) / 1e9,
+        "encode_with_rate_control_GBps": nbytes / (enc_full_ms / 1e3) / 1e9,
+        "region_p50_us": lat[len(lat) // 2], "region_p99_us": lat[min(len(lat) - 1, int(len(lat) * 0.99))],
+        "bit_exact": {"archive_vs_reference": bit_exact_archive, "lod0_vs_reference": lod0_ok},
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = args_parse()
+    dist = Dist()
+    if args.impl == "reference":
+        reference_arm(args, dist)
+    else:
+        gb300_arm(args, dist)
+
+
+if __name__ == "__main__":
+    main()

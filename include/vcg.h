@@ -1,0 +1,74 @@
+// vcg.h — GB300 extensions to the vc.h C API (no counterpart in the reference
+// unless stated). Plain C types only: device buffers are passed as pointers
+// returned by vcg_alloc (or any CUDA device allocation on the same device).
+#ifndef VCG_H
+#define VCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "vc.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Decode into device memory instead of a host buffer (same results and
+// statuses as vc_decode_region / vc_decode_lod). On VC_ERR_FORMAT the contents
+// of out_dev are unspecified.
+vc_status vcg_decode_region_device(vc_archive *a, int lod, vc_box box, uint8_t *out_dev);
+vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev, vc_dims *out_dims);
+
+// Resolve the archive's atom table and copy archive + table into device
+// memory now (otherwise done on the first decode).
+vc_status vcg_make_resident(vc_archive *a);
+
+// vc_encode with the volume already in device memory; *q0 (optional)
+// receives the LOD0 base_q chosen by rate control.
+vc_status vcg_encode_device(const uint8_t *vol_dev, vc_dims dims, float target_ratio,
+                            uint8_t **out_archive, size_t *out_len, float *q0);
+
+// Encode with an explicit base_q per LOD (the reference's vc_set_base_q
+// semantics: each q is clamped to [0.05, 4096]; q <= 0 for a LOD below the
+// volume's LOD count is VC_ERR_RANGE) instead of rate control. vol is host
+// memory, or device memory when vol_on_device is nonzero.
+vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
+                       const float base_q[VC_NLOD], uint8_t **out_archive, size_t *out_len);
+
+// Seeded synthetic scroll-sheet volume (the benchmark workload) generated on
+// the device; byte-identical to the host generator in libvcsynth.
+int vcg_synth_volume_device(uint32_t nx, uint32_t ny, uint32_t nz, uint64_t seed, uint8_t *out_dev);
+
+// Measurement. Each decode / encode call brackets its kernels with CUDA events
+// on its own stream; vcg_last_call_ms returns that device time for the calling
+// thread's last call. With profiling enabled, per-stage device times, launch
+// counts, algorithmic bytes read / written and work units are accumulated per
+// kernel stage and read back (and optionally reset) with vcg_profile_read.
+typedef struct {
+    char name[32];
+    double ms;
+    uint64_t launches;
+    uint64_t bytes_read;
+    uint64_t bytes_written;
+    uint64_t units;
+} vcg_kernel_stat;
+void   vcg_profile_enable(int on);
+int    vcg_profile_read(vcg_kernel_stat *out, int max, int reset);
+double vcg_last_call_ms(void);
+
+// Device / pinned memory helpers (cudaMalloc / cudaMallocHost / cudaMemcpy
+// with direction inferred).
+void *vcg_alloc(size_t bytes);
+void  vcg_free(void *p);
+void *vcg_alloc_host(size_t bytes);
+void  vcg_free_host(void *p);
+int   vcg_copy(void *dst, const void *src, size_t bytes);
+int   vcg_memset(void *dst, int v, size_t bytes);
+int   vcg_sync(void);
+int   vcg_device_info(int *num_sms, int *cc_major, int *cc_minor);
+const char *vcg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif // VCG_H

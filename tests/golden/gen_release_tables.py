@@ -31,7 +31,8 @@ OUT = os.path.join(ROOT, "volume-compressor_gb300", "csrc", "vc_release_tables.h
 def step_tables():
     lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libvcref.so"))
     st = np.zeros(32768, np.float32)
-    lib.refshim_tables(None, st.ctypes.data_as(ctypes.c_void_p), None)
+    cm = np.zeros(1024, np.int32)
+    lib.refshim_tables(cm.ctypes.data_as(ctypes.c_void_p), st.ctypes.data_as(ctypes.c_void_p), None)
     bits = st.view(np.uint32)
     idx = np.arange(32768)
     freq = idx // 1024 + (idx // 32) % 32 + idx % 32
@@ -49,7 +50,7 @@ def step_tables():
         mask[sel] = vals != base[f]
     words = np.packbits(mask.reshape(-1, 8)[:, ::-1], axis=1).reshape(-1)  # LSB-first bytes
     words = words.view(np.uint32)  # little-endian: bit i of word w = raster index 32*w+i
-    return base, alt, words
+    return base, alt, words, cm.reshape(32, 32)
 
 
 def rcp_table():
@@ -70,7 +71,7 @@ def fmt(name, arr, per_line=8):
 
 
 def main():
-    base, alt, mask = step_tables()
+    base, alt, mask, cm = step_tables()
     rcp = rcp_table()
     hdr = [
         "// Generated by tests/golden/gen_release_tables.py from the reference's release",
@@ -92,6 +93,10 @@ def main():
         "// bit (i & 31) of word (i >> 5) set: raster index i uses vc_step_alt_bits[freq(i)]",
         fmt("vc_step_alt_mask", mask),
         fmt("vc_rcp_est_bits", rcp),
+        "// CMATA (src/vc/vc.c:75-88): round(c_k cos(pi (2n+1) k / 64) 2^14), row k = frequency",
+        "#define VC_CMAT_INIT { \\",
+        "\n".join("    {" + ", ".join(str(int(v)) for v in row) + "}, \\" for row in cm),
+        "}",
         "#endif",
         "",
     ]

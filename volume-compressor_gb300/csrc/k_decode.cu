@@ -1,0 +1,255 @@
+// Decode kernels: per-atom list capacities + scan, range-decode lanes, and the
+// fused dequantise + inverse DCT-32 + crop.
+//
+//   k_caps       one thread per box atom: coefficient-list capacity
+//   k_scan_u64   one CTA: exclusive scan of the capacities (list placement)
+//   k_rc_decode  one thread per PRESENT atom: serial range decode of its
+//                payload into (raster index, level) pairs (src/vc/vc.c:545-560)
+//   k_idct       one CTA per atom (persistent over the box): scatter levels into
+//                a 32x32x32 i32 tile in shared memory, dequantise while loading
+//                each z-slab (src/vc/vc.c:327-338), inverse passes along x and y
+//                per slab (warp per slab, lane per line), then along z (lane per
+//                column), add dc, clamp to u8 and store the cropped voxels
+//                (src/vc/vc.c:219-229, 1535-1555)
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dct32.cuh"
+#include "kernels.cuh"
+#include "rangecoder.cuh"
+
+namespace vcg {
+
+constexpr int kIdctThreads = 256;
+constexpr size_t kIdctSmem = 32768 * sizeof(int32_t);
+
+__global__ void k_caps(DecodeJob J) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J.n_atoms) return;
+    uint32_t az, ay, ax;
+    box_atom(J, t, az, ay, ax);
+    vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
+    uint64_t cap = 0;
+    if (e.kind == VCD_PRESENT) {
+        cap = 8ull * (e.len - 1) + 64ull;
+        if (cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+    }
+    J.ent_off[t] = cap;
+}
+
+// Exclusive scan of v[0..n) in place (+ base), total -> *total. One CTA of 1024
+// threads walks the array in tiles of 4096 carrying the running sum.
+__global__ void __launch_bounds__(1024) k_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total) {
+    __shared__ uint64_t warp_sum[32];
+    __shared__ uint64_t carry_s;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry_s = base;
+    __syncthreads();
+    for (uint64_t tile = 0; tile < n; tile += 4096) {
+        uint64_t i0 = tile + (uint64_t)tid * 4;
+        uint64_t a[4];
+        uint64_t s = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            a[j] = (i0 + j < n) ? v[i0 + j] : 0;
+            uint64_t x = a[j];
+            a[j] = s;
+            s += x;
+        }
+        uint64_t incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sum[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint64_t w = warp_sum[lane], wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint64_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            warp_sum[lane] = wi - w;   // exclusive prefix of warp totals
+        }
+        __syncthreads();
+        uint64_t excl = carry_s + warp_sum[wid] + (incl - s);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (i0 + j < n) v[i0 + j] = excl + a[j];
+        __syncthreads();
+        if (tid == 1023) carry_s = excl + s;
+        __syncthreads();
+    }
+    if (tid == 0 && total) *total = carry_s;
+}
+
+__global__ void __launch_bounds__(128) k_rc_decode(DecodeJob J) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J.n_atoms) return;
+    uint32_t az, ay, ax;
+    box_atom(J, t, az, ay, ax);
+    vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
+    if (e.kind != VCD_PRESENT) { J.cnt[t] = 0; return; }
+    uint32_t cap = 8u * (e.len - 1u) + 64u;
+    if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+    uint32_t *dst = J.ent + J.ent_off[t];
+    const uint16_t *scan = J.scan;
+    RcDec d;
+    d.init(J.arc + e.off + 1, e.len - 1);
+    uint32_t n = 0;
+    int bad = rc_decode_levels(d, J.band_start, [&](uint32_t p, uint32_t lv) {
+        if (n < cap) dst[n] = (uint32_t)__ldg(scan + p) | (lv << 16);
+        ++n;
+    });
+    uint32_t flags = (n > cap ? kEntOverflow : 0u) | (bad ? kEntBad : 0u);
+    J.cnt[t] = (n > cap ? cap : n) | flags;
+    atomicAdd(J.nnz_total, (unsigned long long)(n > cap ? cap : n));
+    if (bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
+}
+
+__device__ __forceinline__ int tile_idx(uint32_t r) {   // raster (kz,ky,kx) -> swizzled slab slot
+    return (int)((r >> 10) << 10) | swz((int)((r >> 5) & 31u), (int)(r & 31u));
+}
+
+// dequantised coefficient of raw level l at raster r (src/vc/vc.c:327-338, i32 wrap)
+__device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t *dqs, const int32_t *dqb,
+                                           const uint32_t *alt) {
+    uint32_t f = (r >> 10) + ((r >> 5) & 31u) + (r & 31u);
+    uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
+    uint32_t m = (uint32_t)(l < 0 ? -l : l);
+    int32_t v = (int32_t)(m * (uint32_t)dqs[cls] + (uint32_t)dqb[cls] + 128u) >> 8;
+    return l == 0 ? 0 : (l < 0 ? (int32_t)(0u - (uint32_t)v) : v);
+}
+
+__global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
+    extern __shared__ int32_t T[];   // 32 slabs x swizzled 32x32
+    __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
+    __shared__ uint32_t alt[1024];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < VCD_NCLASS; i += kIdctThreads) { dqs[i] = J.dq->step[i]; dqb[i] = J.dq->bias[i]; }
+    for (int i = tid; i < 1024; i += kIdctThreads) alt[i] = J.alt_mask[i];
+    __syncthreads();
+
+    for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
+        uint32_t az, ay, ax;
+        box_atom(J, t, az, ay, ax);
+        const vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
+        // crop window of this atom inside the box, atom-local coordinates
+        const uint32_t gx = ax * 32, gy = ay * 32, gz = az * 32;
+        const uint32_t lx0 = J.x0 > gx ? J.x0 - gx : 0, lx1 = J.x1 < gx + 32 ? J.x1 - gx : 32;
+        const uint32_t ly0 = J.y0 > gy ? J.y0 - gy : 0, ly1 = J.y1 < gy + 32 ? J.y1 - gy : 32;
+        const uint32_t lz0 = J.z0 > gz ? J.z0 - gz : 0, lz1 = J.z1 < gz + 32 ? J.z1 - gz : 32;
+        uint8_t *obase = J.out + ((uint64_t)(gz + lz0 - J.z0) * J.oy + (gy + ly0 - J.y0)) * J.ox + (gx + lx0 - J.x0);
+        const uint32_t cw = lx1 - lx0, ch = ly1 - ly0, cd = lz1 - lz0;
+        const uint32_t c = e.kind == VCD_PRESENT ? J.cnt[t] : kEntBad;
+        if (e.kind != VCD_PRESENT || (c & kEntBad)) {   // ABSENT / KNOWN_ZERO -> zeros
+            for (uint32_t i = tid; i < cw * ch * cd; i += kIdctThreads) {
+                uint32_t x = i % cw, y = (i / cw) % ch, z = i / (cw * ch);
+                obase[((uint64_t)z * J.oy + y) * J.ox + x] = 0;
+            }
+            continue;
+        }
+        const int32_t dc = J.arc[e.off];
+        int4 *T4 = reinterpret_cast<int4 *>(T);
+        for (int i = tid; i < 32768 / 4; i += kIdctThreads) T4[i] = make_int4(0, 0, 0, 0);
+        __syncthreads();
+        if (c & kEntOverflow) {
+            // slow path for streams whose list exceeded its capacity
+            if (tid == 0) {
+                RcDec d;
+                d.init(J.arc + e.off + 1, e.len - 1);
+                rc_decode_levels(d, J.band_start, [&](uint32_t p, uint32_t lv) {
+                    T[tile_idx(J.scan[p])] = (int16_t)lv;
+                });
+            }
+        } else {
+            const uint32_t n = c & kEntMask;
+            const uint32_t *src = J.ent + J.ent_off[t];
+            for (uint32_t i = tid; i < n; i += kIdctThreads) {
+                uint32_t w = src[i];
+                T[tile_idx(w & 0xFFFFu)] = (int16_t)(w >> 16);
+            }
+        }
+        __syncthreads();
+
+        // passes along x then y, one warp per z-slab
+        for (int kz = warp; kz < 32; kz += kIdctThreads / 32) {
+            int32_t *S = T + kz * 1024;
+            int32_t v[32], o[32];
+            int any = 0;
+#pragma unroll
+            for (int kx = 0; kx < 32; ++kx) {
+                int32_t l = S[swz(lane, kx)];
+                v[kx] = dequant(l, (uint32_t)(kz * 1024 + lane * 32 + kx), dqs, dqb, alt);
+                any |= v[kx];
+            }
+            if (__any_sync(0xFFFFFFFFu, any)) {
+                idct32_line(v, o);
+#pragma unroll
+                for (int x = 0; x < 32; ++x) S[swz(lane, x)] = o[x];
+                __syncwarp();
+#pragma unroll
+                for (int ky = 0; ky < 32; ++ky) v[ky] = S[swz(ky, lane)];
+                idct32_line(v, o);
+                __syncwarp();
+#pragma unroll
+                for (int y = 0; y < 32; ++y) S[swz(y, lane)] = o[y];
+            } else {
+#pragma unroll
+                for (int x = 0; x < 32; ++x) S[swz(lane, x)] = 0;
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+
+        // pass along z: thread = column (y, x = lane); store the cropped voxels
+        for (int y = warp; y < 32; y += kIdctThreads / 32) {
+            int32_t v[32], o[32];
+#pragma unroll
+            for (int kz = 0; kz < 32; ++kz) v[kz] = T[kz * 1024 + swz(y, lane)];
+            idct32_line(v, o);
+            const bool in_xy = (uint32_t)lane >= lx0 && (uint32_t)lane < lx1 && (uint32_t)y >= ly0 && (uint32_t)y < ly1;
+            if (in_xy) {
+                uint8_t *col = obase + (uint64_t)(y - ly0) * J.ox + (lane - lx0);
+#pragma unroll
+                for (int z = 0; z < 32; ++z) {
+                    if ((uint32_t)z >= lz0 && (uint32_t)z < lz1) {
+                        int32_t x = (int32_t)((uint32_t)o[z] + (uint32_t)dc);
+                        col[(uint64_t)(z - lz0) * J.oy * J.ox] = (uint8_t)(x < 0 ? 0 : x > 255 ? 255 : x);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cudaStream_t s) {
+    k_scan_u64<<<1, 1024, 0, s>>>(v, n, base, total);
+}
+
+void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_idct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIdctSmem);
+        attr = true;
+    }
+    if (ev) cudaEventRecord(ev->ev[0], s);
+    unsigned nb = (unsigned)((J.n_atoms + 127) / 128);
+    if (J.n_atoms) {
+        k_caps<<<nb, 128, 0, s>>>(J);
+        launch_scan_u64(J.ent_off, J.n_atoms, 0, nullptr, s);
+    }
+    if (ev) cudaEventRecord(ev->ev[1], s);
+    if (J.n_atoms) k_rc_decode<<<nb, 128, 0, s>>>(J);
+    if (ev) cudaEventRecord(ev->ev[2], s);
+    if (J.n_atoms) {
+        uint64_t grid = J.n_atoms < (uint64_t)num_sms ? J.n_atoms : (uint64_t)num_sms;
+        k_idct<<<(unsigned)grid, kIdctThreads, kIdctSmem, s>>>(J);
+    }
+    if (ev) cudaEventRecord(ev->ev[3], s);
+}
+
+}  // namespace vcg

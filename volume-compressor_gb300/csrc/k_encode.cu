@@ -1,0 +1,302 @@
+// Encode kernels.
+//
+//   k_downsample  LOD k -> k+1: integer mean of the in-bounds 2x2x2 children,
+//                 (acc + n/2) / n (src/vc/vc.c:1562-1577)
+//   k_fwd         one CTA per atom: gather (zero padding outside the volume),
+//                 sum -> zero flag + dc (src/vc/vc.c:599-604), forward DCT-32
+//                 passes x, y per z-slab then z per column (src/vc/vc.c:212-218),
+//                 dead-zone quantiser as the release build evaluates it
+//                 (src/vc/vc.c:293-306), levels scattered to scan order in
+//                 shared memory and compacted to (scan position, level) lists
+//   k_rc_encode   one thread per atom: range coder, size-only or writing the
+//                 payload [dc][bytes] at its archive offset (src/vc/vc.c:528-544,
+//                 595-622)
+//   k_consume / k_slots   canonical layout: bytes consumed per atom in append
+//                 order (an L2 block of 512 KiB at a region's first atom, then the
+//                 payload) and the 16-byte L2 slots (src/vc/vc.c:1082-1159)
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dct32.cuh"
+#include "k_encode.cuh"
+#include "rangecoder.cuh"
+
+namespace vcg {
+
+constexpr int kFwdThreads = 256;
+constexpr size_t kFwdSmem = 32768 * sizeof(int32_t) + 32768 * sizeof(int16_t);
+
+__global__ void k_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out) {
+    const uint32_t ox = (nx + 1) / 2, oy = (ny + 1) / 2, oz = (nz + 1) / 2;
+    const uint64_t n = (uint64_t)ox * oy * oz;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x = (uint32_t)(i % ox), y = (uint32_t)((i / ox) % oy), z = (uint32_t)(i / ((uint64_t)ox * oy));
+        uint32_t acc = 0, cnt = 0;
+        for (uint32_t zz = 2 * z; zz < 2 * z + 2 && zz < nz; ++zz)
+            for (uint32_t yy = 2 * y; yy < 2 * y + 2 && yy < ny; ++yy) {
+                const uint8_t *row = in + ((uint64_t)zz * ny + yy) * nx;
+                acc += row[2 * x];
+                ++cnt;
+                if (2 * x + 1 < nx) { acc += row[2 * x + 1]; ++cnt; }
+            }
+        out[i] = (uint8_t)((acc + cnt / 2) / cnt);
+    }
+}
+
+// 32 voxels of row (z, y) of atom (az, ay, ax), zero outside the volume, packed
+// little-endian into 8 words.
+__device__ __forceinline__ void load_row(const uint8_t *vol, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t gx,
+                                         uint32_t gy, uint32_t gz, uint32_t (&w)[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) w[i] = 0;
+    if (gy >= ny || gz >= nz || gx >= nx) return;
+    const uint8_t *p = vol + ((uint64_t)gz * ny + gy) * nx + gx;
+    if (gx + 32 <= nx && ((uintptr_t)p & 15u) == 0) {
+        uint4 a = __ldg(reinterpret_cast<const uint4 *>(p));
+        uint4 b = __ldg(reinterpret_cast<const uint4 *>(p + 16));
+        w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w; w[4] = b.x; w[5] = b.y; w[6] = b.z; w[7] = b.w;
+        return;
+    }
+    uint32_t cnt = nx - gx < 32 ? nx - gx : 32;
+    for (uint32_t i = 0; i < cnt; ++i) w[i >> 2] |= (uint32_t)__ldg(p + i) << (8 * (i & 3));
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
+    extern __shared__ int32_t smem[];
+    int32_t *T = smem;                                          // 32 slabs x swizzled 32x32
+    int16_t *L = reinterpret_cast<int16_t *>(smem + 32768);     // levels in scan order
+    __shared__ float qdz[VCD_NCLASS], qrr[VCD_NCLASS];
+    __shared__ uint16_t rank[94 * 32];
+    __shared__ uint32_t alt[1024];
+    __shared__ uint32_t red[32];
+    __shared__ uint32_t scanbuf[kFwdThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q.dz[i]; qrr[i] = J.q.rr[i]; }
+    for (int i = tid; i < 94 * 32; i += kFwdThreads) rank[i] = J.rank_base[i];
+    for (int i = tid; i < 1024; i += kFwdThreads) alt[i] = J.alt_mask[i];
+
+    for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
+        const uint64_t a = J.first_atom + t;   // raster atom index within the LOD
+        const uint32_t ax = (uint32_t)(a % J.acx), ay = (uint32_t)((a / J.acx) % J.acy),
+                       az = (uint32_t)(a / ((uint64_t)J.acx * J.acy));
+        // rows r = tid + 256 j: z = r >> 5, y = r & 31 (lane)
+        uint32_t w[4][8];
+        uint32_t s = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int r = tid + kFwdThreads * j;
+            load_row(J.vol, J.nx, J.ny, J.nz, ax * 32, ay * 32 + (r & 31), az * 32 + (r >> 5), w[j]);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s = __dp4a(w[j][i], 0x01010101u, s);
+        }
+        // zero the scan-order level buffer while the sum reduces
+        int4 *L4 = reinterpret_cast<int4 *>(L);
+        for (int i = tid; i < 32768 * 2 / 16; i += kFwdThreads) L4[i] = make_int4(0, 0, 0, 0);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+        if (lane == 0) red[warp] = s;
+        __syncthreads();
+        uint32_t sum = 0;
+#pragma unroll
+        for (int i = 0; i < kFwdThreads / 32; ++i) sum += red[i];
+        if (sum == 0) {   // all-zero atom: no payload (src/vc/vc.c:601)
+            if (tid == 0) J.meta[t] = kMetaZero;
+            __syncthreads();
+            continue;
+        }
+        const int32_t dc = (int32_t)((sum + 16384u) / 32768u);
+        // pass along x for the thread's 4 rows, straight from registers
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int r = tid + kFwdThreads * j;
+            int32_t v[32], o[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = (int32_t)((w[j][i >> 2] >> (8 * (i & 3))) & 0xFFu) - dc;
+            fdct32_line(v, o);
+            int32_t *S = T + (r >> 5) * 1024;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) S[swz(r & 31, k)] = o[k];
+        }
+        __syncthreads();
+        // pass along y, warp per z-slab, lane per column kx
+        for (int z = warp; z < 32; z += kFwdThreads / 32) {
+            int32_t *S = T + z * 1024;
+            int32_t v[32], o[32];
+#pragma unroll
+            for (int y = 0; y < 32; ++y) v[y] = S[swz(y, lane)];
+            fdct32_line(v, o);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) S[swz(k, lane)] = o[k];
+        }
+        __syncthreads();
+        // pass along z per column (ky, kx = lane), quantise, scatter to scan order
+        for (int ky = warp; ky < 32; ky += kFwdThreads / 32) {
+            int32_t v[32], o[32];
+#pragma unroll
+            for (int z = 0; z < 32; ++z) v[z] = T[z * 1024 + swz(ky, lane)];
+            fdct32_line(v, o);
+#pragma unroll
+            for (int kz = 0; kz < 32; ++kz) {
+                const int32_t cf = o[kz];
+                const uint32_t f = (uint32_t)(kz + ky + lane);
+                const uint32_t r = (uint32_t)(kz * 1024 + ky * 32 + lane);
+                const uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
+                const uint32_t mag = cf < 0 ? 0u - (uint32_t)cf : (uint32_t)cf;
+                const float fa = __int2float_rn((int32_t)mag);
+                int32_t level = 0;
+                if (fa >= qdz[cls]) {
+                    level = __float2int_rz(__fadd_rn(__fmul_rn(__fsub_rn(fa, qdz[cls]), qrr[cls]), 1.0f));
+                    if (level > 32767) level = 32767;
+                }
+                if (level) {
+                    int sub = (int)f - kz - 31;
+                    uint32_t p = (uint32_t)rank[f * 32 + kz] + (uint32_t)ky - (uint32_t)(sub > 0 ? sub : 0);
+                    L[p] = (int16_t)(cf < 0 ? -level : level);
+                }
+            }
+        }
+        __syncthreads();
+        // compaction in scan order: thread owns positions [128 tid, 128 tid + 128)
+        const uint4 *Lv = reinterpret_cast<const uint4 *>(L + tid * 128);
+        uint32_t cnt = 0;
+#pragma unroll 4
+        for (int i = 0; i < 16; ++i) {
+            uint4 q = Lv[i];
+            uint32_t ws[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) cnt += ((ws[k] & 0xFFFFu) != 0) + ((ws[k] >> 16) != 0);
+        }
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) scanbuf[warp] = incl;
+        __syncthreads();
+        uint32_t base = 0, total = 0;
+#pragma unroll
+        for (int i = 0; i < kFwdThreads / 32; ++i) {
+            uint32_t v = scanbuf[i];
+            base += i < warp ? v : 0;
+            total += v;
+        }
+        base += incl - cnt;
+        uint32_t *dst = J.ent + t * (uint64_t)VCD_MAX_ENTRIES + base;
+        if (cnt) {
+#pragma unroll 4
+            for (int i = 0; i < 16; ++i) {
+                uint4 q = Lv[i];
+                uint32_t ws[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    uint32_t p = (uint32_t)(tid * 128 + i * 8 + k * 2);
+                    if (ws[k] & 0xFFFFu) *dst++ = p | (ws[k] << 16);
+                    if (ws[k] >> 16) *dst++ = (p + 1) | (ws[k] & 0xFFFF0000u);
+                }
+            }
+        }
+        if (tid == 0) J.meta[t] = total | ((uint32_t)dc << 16);
+        __syncthreads();
+    }
+}
+
+template <bool WRITE>
+__global__ void __launch_bounds__(128) k_rc_encode(RcJob J) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J.n_atoms) return;
+    const uint32_t meta = J.meta[t];
+    if (meta & kMetaZero) {
+        if (!WRITE) J.len[t] = 0;
+        return;
+    }
+    const uint32_t nnz = meta & 0xFFFFu;
+    const uint32_t *ent = J.ent + t * (uint64_t)VCD_MAX_ENTRIES;
+    if (!WRITE) {
+        uint32_t n = rc_encode_levels<false>(ent, nnz, J.band_start, nullptr);
+        J.len[t] = n + 1;
+        atomicAdd(J.total_bytes, (unsigned long long)(n + 1));
+        atomicAdd(J.total_present, 1ull);
+        return;
+    }
+    const uint64_t a = J.canon_first + t;   // canonical index
+    const uint64_t off = J.pos[a] + (J.lay.first_in_region(a) ? kL2Bytes : 0ull);
+    uint8_t *dst = J.arc + off;
+    dst[0] = (uint8_t)((meta >> 16) & 0xFFu);
+    rc_encode_levels<true>(ent, nnz, J.band_start, dst + 1);
+}
+
+// consume[a] = (first atom of its region ? L2 block : 0) + payload length
+__global__ void k_consume(PlaceJob J) {
+    uint64_t a = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= J.n_total) return;
+    J.pos[a] = (J.lay.first_in_region(a) ? kL2Bytes : 0ull) + J.len[a];
+}
+
+__global__ void k_slots(PlaceJob J) {
+    uint64_t a = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= J.n_total) return;
+    int lod;
+    uint32_t az, ay, ax;
+    J.lay.coords(a, lod, az, ay, ax);
+    const uint64_t blk = J.pos[J.lay.region_first(lod, az, ay, ax)];
+    uint8_t *slot = J.arc + blk + ((((uint64_t)(az & 31) * 32 + (ay & 31)) * 32 + (ax & 31)) * 16);
+    const uint32_t len = J.len[a];
+    uint4 v;
+    if (len == 0) {   // known-zero atom (src/vc/vc.c:1133-1141)
+        v = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 2u);
+    } else {
+        const uint64_t off = J.pos[a] + (J.lay.first_in_region(a) ? kL2Bytes : 0ull);
+        v = make_uint4((uint32_t)off, (uint32_t)(off >> 32), len, 1u | ((J.dc[a] & 0xFFu) << 8));
+    }
+    // an L2 block starts wherever the cursor was (any byte offset): store bytewise
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 16; ++i) slot[i] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
+}
+
+__global__ void k_gather_dc(const uint32_t *meta, uint64_t n, uint8_t *dc) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dc[t] = (meta[t] & kMetaZero) ? 0 : (uint8_t)(meta[t] >> 16);
+}
+
+void enc_set_smem() {
+    static bool done = false;
+    if (!done) {
+        cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+        done = true;
+    }
+}
+
+void launch_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, int num_sms,
+                       cudaStream_t s) {
+    k_downsample<<<num_sms * 8, 256, 0, s>>>(in, nx, ny, nz, out);
+}
+
+void launch_fwd(const FwdJob &J, int num_sms, cudaStream_t s) {
+    enc_set_smem();
+    if (!J.n_atoms) return;
+    uint64_t grid = J.n_atoms < (uint64_t)num_sms ? J.n_atoms : (uint64_t)num_sms;
+    k_fwd<<<(unsigned)grid, kFwdThreads, kFwdSmem, s>>>(J);
+}
+
+void launch_rc_encode(const RcJob &J, bool write, cudaStream_t s) {
+    if (!J.n_atoms) return;
+    unsigned nb = (unsigned)((J.n_atoms + 127) / 128);
+    if (write) k_rc_encode<true><<<nb, 128, 0, s>>>(J);
+    else k_rc_encode<false><<<nb, 128, 0, s>>>(J);
+}
+
+void launch_consume(const PlaceJob &J, cudaStream_t s) {
+    k_consume<<<(unsigned)((J.n_total + 255) / 256), 256, 0, s>>>(J);
+}
+
+void launch_slots(const PlaceJob &J, cudaStream_t s) {
+    k_slots<<<(unsigned)((J.n_total + 255) / 256), 256, 0, s>>>(J);
+}
+
+void launch_gather_dc(const uint32_t *meta, uint64_t n, uint8_t *dc, cudaStream_t s) {
+    k_gather_dc<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(meta, n, dc);
+}
+
+}  // namespace vcg

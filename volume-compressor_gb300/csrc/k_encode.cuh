@@ -1,0 +1,85 @@
+// Encode kernel interfaces (private).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vc_internal.h"
+
+namespace vcg {
+
+constexpr uint64_t kL2Bytes = 32768ull * 16ull;   // one region's slot block
+constexpr uint32_t kMetaZero = 1u << 31;           // meta: all-zero atom
+// meta = nnz (bits 0-15, up to 32768) | dc << 16 | kMetaZero
+
+// Canonical append order: LOD-major, atoms in raster (z, y, x) order.
+struct Layout {
+    int nlod;
+    uint64_t base[9];
+    uint32_t acx[8], acy[8], acz[8];
+
+    __host__ __device__ void coords(uint64_t a, int &lod, uint32_t &az, uint32_t &ay, uint32_t &ax) const {
+        lod = 0;
+        while (lod + 1 < nlod && a >= base[lod + 1]) ++lod;
+        uint64_t l = a - base[lod];
+        ax = (uint32_t)(l % acx[lod]);
+        ay = (uint32_t)((l / acx[lod]) % acy[lod]);
+        az = (uint32_t)(l / ((uint64_t)acx[lod] * acy[lod]));
+    }
+    __host__ __device__ bool first_in_region(uint64_t a) const {
+        int lod;
+        uint32_t az, ay, ax;
+        coords(a, lod, az, ay, ax);
+        return ((az | ay | ax) & 31u) == 0;
+    }
+    __host__ __device__ uint64_t region_first(int lod, uint32_t az, uint32_t ay, uint32_t ax) const {
+        return base[lod] + ((uint64_t)(az & ~31u) * acy[lod] + (ay & ~31u)) * acx[lod] + (ax & ~31u);
+    }
+};
+
+struct FwdJob {
+    const uint8_t *vol;          // LOD volume (x fastest)
+    uint32_t nx, ny, nz;
+    uint32_t acx, acy;
+    uint64_t first_atom;         // raster index within the LOD of this chunk's first atom
+    uint64_t n_atoms;
+    vcd_quant q;                 // per-class quantiser constants
+    const uint16_t *rank_base;
+    const uint32_t *alt_mask;
+    uint32_t *ent;               // per atom VCD_MAX_ENTRIES slots: scan position | level << 16
+    uint32_t *meta;              // per atom
+};
+
+struct RcJob {
+    uint64_t n_atoms;
+    const uint32_t *meta;
+    const uint32_t *ent;
+    uint32_t band_start[9];
+    // size pass
+    uint32_t *len;                       // payload bytes per atom ([dc] + coder bytes; 0 = zero atom)
+    unsigned long long *total_bytes;
+    unsigned long long *total_present;
+    // write pass
+    uint8_t *arc;
+    const uint64_t *pos;                 // canonical exclusive scan of consumed bytes
+    uint64_t canon_first;                // canonical index of this chunk's first atom
+    Layout lay;
+};
+
+struct PlaceJob {
+    uint64_t n_total;
+    uint64_t *pos;                       // in: consume; out after scan: cursor before each atom
+    const uint32_t *len;
+    const uint8_t *dc;
+    uint8_t *arc;
+    Layout lay;
+};
+
+void launch_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, int num_sms,
+                       cudaStream_t s);
+void launch_fwd(const FwdJob &J, int num_sms, cudaStream_t s);
+void launch_rc_encode(const RcJob &J, bool write, cudaStream_t s);
+void launch_consume(const PlaceJob &J, cudaStream_t s);
+void launch_slots(const PlaceJob &J, cudaStream_t s);
+void launch_gather_dc(const uint32_t *meta, uint64_t n, uint8_t *dc, cudaStream_t s);
+
+}  // namespace vcg

@@ -1,0 +1,51 @@
+// Kernel interfaces shared by the CUDA translation units (private).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vc_internal.h"
+
+namespace vcg {
+
+constexpr uint32_t kEntOverflow = 1u << 31;   // cnt flag: list exceeded its capacity
+constexpr uint32_t kEntBad = 1u << 30;        // cnt flag: malformed stream
+constexpr uint32_t kEntMask = (1u << 30) - 1u;
+
+// Region / LOD decode, box atoms in (z, y, x) order.
+struct DecodeJob {
+    const uint8_t *arc;          // device archive bytes
+    const vcd_atom *atoms;       // device atom table of the LOD
+    uint32_t acx, acy;           // LOD atom grid (x, y)
+    uint32_t bax, bay, baz, bnx, bny;
+    uint64_t n_atoms;
+    uint32_t x0, y0, z0, x1, y1, z1;   // box
+    uint8_t *out;                // box raster (x fastest)
+    uint64_t ox, oy;             // box extent x, y
+    uint32_t *ent;               // coefficient lists: raster index | level << 16
+    uint64_t *ent_off;           // per box atom: first list slot (after the scan)
+    uint32_t *cnt;               // per box atom: entries | flags
+    const vcd_dq *dq;            // dequant tables of the LOD
+    const uint32_t *alt_mask;    // step-class alternate bits
+    const uint16_t *scan;        // scan position -> raster
+    uint32_t *err;               // lowest malformed box atom (atomicMin)
+    unsigned long long *nnz_total;   // coefficient-list entries written (sum over atoms)
+    uint32_t band_start[9];      // first scan position of each significance band
+};
+
+// Optional per-stage events: ev[0] before the list placement, ev[1] before the
+// range decoder, ev[2] before the inverse transform, ev[3] after it.
+struct StageEvents {
+    cudaEvent_t ev[4];
+};
+
+__host__ __device__ inline void box_atom(const DecodeJob &J, uint64_t t, uint32_t &az, uint32_t &ay,
+                                         uint32_t &ax) {
+    ax = J.bax + (uint32_t)(t % J.bnx);
+    ay = J.bay + (uint32_t)((t / J.bnx) % J.bny);
+    az = J.baz + (uint32_t)(t / ((uint64_t)J.bnx * J.bny));
+}
+
+void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev);
+void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cudaStream_t s);
+
+}  // namespace vcg

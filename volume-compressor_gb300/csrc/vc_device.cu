@@ -1,0 +1,315 @@
+// Device runtime: one CUDA context per process, one stream + grow-only scratch
+// per host thread, archive residency, and the decode orchestration.
+#include <cuda_runtime.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "kernels.cuh"
+#include "vc_device.h"
+
+using namespace vcg;
+
+// ---------------------------------------------------------------- errors
+static __thread char g_err[256];
+extern "C" const char *vcd_last_error(void) { return g_err; }
+void vcd_set_error(const char *what, cudaError_t e) {
+    snprintf(g_err, sizeof g_err, "%s: %s", what, e == cudaSuccess ? "failed" : cudaGetErrorString(e));
+}
+int vcd_status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? 3 /*VC_ERR_OOM*/ : 4 /*VC_ERR_IO*/; }
+
+// ---------------------------------------------------------------- process context
+static pthread_once_t g_once = PTHREAD_ONCE_INIT;
+static int g_init_rc = -1;
+vcd_device g_dev;
+
+static void init_once(void) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n <= 0) { vcd_set_error("cudaGetDeviceCount", e); return; }
+    int dev = 0;
+    const char *env = getenv("VC_DEVICE");
+    if (env) dev = atoi(env);
+    if ((e = cudaSetDevice(dev)) != cudaSuccess) { vcd_set_error("cudaSetDevice", e); return; }
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, dev)) != cudaSuccess) { vcd_set_error("cudaGetDeviceProperties", e); return; }
+    if (prop.major < 10) {
+        snprintf(g_err, sizeof g_err, "device %d (sm_%d%d) cannot run sm_103a code", dev, prop.major, prop.minor);
+        return;
+    }
+    g_dev.device = dev;
+    g_dev.num_sms = prop.multiProcessorCount;
+    vcd_tables *t = (vcd_tables *)malloc(sizeof(vcd_tables));
+    vch_tables(t);
+    memcpy(g_dev.band_start, t->band_start, sizeof g_dev.band_start);
+    if ((e = cudaMalloc(&g_dev.tables, sizeof(vcd_tables))) != cudaSuccess ||
+        (e = cudaMemcpy(g_dev.tables, t, sizeof(vcd_tables), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        vcd_set_error("table upload", e);
+        free(t);
+        return;
+    }
+    free(t);
+    g_init_rc = 0;
+}
+
+extern "C" int vcd_init(void) {
+    pthread_once(&g_once, init_once);
+    if (g_init_rc == 0) cudaSetDevice(g_dev.device);
+    return g_init_rc;
+}
+
+// ---------------------------------------------------------------- per-thread context
+static pthread_key_t g_ctx_key;
+static pthread_once_t g_key_once = PTHREAD_ONCE_INIT;
+
+static void ctx_free(void *p) {
+    vcd_ctx *c = (vcd_ctx *)p;
+    if (!c) return;
+    for (int i = 0; i < VCD_NBUF; ++i)
+        if (c->buf[i]) cudaFree(c->buf[i]);
+    if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    free(c);
+}
+static void key_once(void) { pthread_key_create(&g_ctx_key, ctx_free); }
+
+vcd_ctx *vcd_thread_ctx(void) {
+    pthread_once(&g_key_once, key_once);
+    vcd_ctx *c = (vcd_ctx *)pthread_getspecific(g_ctx_key);
+    if (c) return c;
+    c = (vcd_ctx *)calloc(1, sizeof(vcd_ctx));
+    cudaSetDevice(g_dev.device);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { vcd_set_error("cudaStreamCreate", e); free(c); return NULL; }
+    for (int i = 0; i < 8; ++i) cudaEventCreate(&c->ev[i]);
+    pthread_setspecific(g_ctx_key, c);
+    return c;
+}
+
+// ---------------------------------------------------------------- profiling
+struct vcd_stat {
+    char name[32];
+    double ms;
+    uint64_t launches, bytes_read, bytes_written, units;
+};
+static vcd_stat g_stats[32];
+static int g_nstats, g_prof;
+static pthread_mutex_t g_stat_mu = PTHREAD_MUTEX_INITIALIZER;
+
+int vcd_prof_on(void) { return g_prof; }
+
+float vcd_elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+void vcd_prof_add(const char *name, double ms, uint64_t launches, uint64_t br, uint64_t bw, uint64_t units) {
+    pthread_mutex_lock(&g_stat_mu);
+    int i = 0;
+    while (i < g_nstats && strcmp(g_stats[i].name, name)) ++i;
+    if (i == g_nstats && g_nstats < 32) {
+        memset(&g_stats[i], 0, sizeof g_stats[i]);
+        snprintf(g_stats[i].name, sizeof g_stats[i].name, "%s", name);
+        ++g_nstats;
+    }
+    if (i < 32) {
+        g_stats[i].ms += ms;
+        g_stats[i].launches += launches;
+        g_stats[i].bytes_read += br;
+        g_stats[i].bytes_written += bw;
+        g_stats[i].units += units;
+    }
+    pthread_mutex_unlock(&g_stat_mu);
+}
+
+extern "C" __attribute__((visibility("default"))) void vcg_profile_enable(int on) { g_prof = on; }
+
+// Copies up to max accumulated kernel statistics into out (layout of
+// vcg_kernel_stat in vcg.h); returns how many exist; reset clears them.
+extern "C" __attribute__((visibility("default"))) int vcg_profile_read(void *out, int max, int reset) {
+    pthread_mutex_lock(&g_stat_mu);
+    int n = g_nstats;
+    if (out) memcpy(out, g_stats, sizeof(vcd_stat) * (size_t)(n < max ? n : max));
+    if (reset) g_nstats = 0;
+    pthread_mutex_unlock(&g_stat_mu);
+    return n;
+}
+
+extern "C" __attribute__((visibility("default"))) double vcg_last_call_ms(void) {
+    vcd_ctx *c = vcd_thread_ctx();
+    return c ? c->last_ms : -1.0;
+}
+
+// grow-only scratch buffer `slot` of the calling thread
+cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out) {
+    if (bytes == 0) bytes = 16;
+    if (c->cap[slot] < bytes) {
+        if (c->buf[slot]) {
+            cudaStreamSynchronize(c->stream);
+            cudaFree(c->buf[slot]);
+            c->buf[slot] = NULL;
+            c->cap[slot] = 0;
+        }
+        size_t want = bytes + bytes / 8;
+        cudaError_t e = cudaMalloc(&c->buf[slot], want);
+        if (e != cudaSuccess) return e;
+        c->cap[slot] = want;
+    }
+    *out = c->buf[slot];
+    return cudaSuccess;
+}
+
+cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out) {
+    if (c->pinned_cap < bytes) {
+        if (c->pinned) cudaFreeHost(c->pinned);
+        c->pinned = NULL;
+        c->pinned_cap = 0;
+        cudaError_t e = cudaMallocHost(&c->pinned, bytes);
+        if (e != cudaSuccess) return e;
+        c->pinned_cap = bytes;
+    }
+    *out = c->pinned;
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------- archive residency
+struct vcd_archive {
+    uint8_t *arc;       // archive bytes (+16 slack)
+    size_t len;
+    vcd_atom *atoms;    // all LODs
+    vcd_dq *dq;         // per LOD
+    int nlod;
+};
+
+extern "C" int vcd_upload_archive(vcd_archive **out, const uint8_t *buf, size_t len, const vcd_atom *atoms,
+                                  uint64_t n_atoms, const vcd_dq *dq, int nlod) {
+    vcd_archive *d = (vcd_archive *)calloc(1, sizeof(vcd_archive));
+    cudaError_t e;
+    if ((e = cudaMalloc(&d->arc, len + 16)) != cudaSuccess ||
+        (e = cudaMemcpy(d->arc, buf, len, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemset(d->arc + len, 0, 16)) != cudaSuccess ||
+        (e = cudaMalloc(&d->atoms, (n_atoms ? n_atoms : 1) * sizeof(vcd_atom))) != cudaSuccess ||
+        (e = cudaMemcpy(d->atoms, atoms, n_atoms * sizeof(vcd_atom), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMalloc(&d->dq, nlod * sizeof(vcd_dq))) != cudaSuccess ||
+        (e = cudaMemcpy(d->dq, dq, nlod * sizeof(vcd_dq), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        vcd_set_error("archive upload", e);
+        vcd_free_archive(d);
+        return vcd_status_of(e);
+    }
+    d->len = len;
+    d->nlod = nlod;
+    *out = d;
+    return 0;
+}
+
+extern "C" void vcd_free_archive(vcd_archive *d) {
+    if (!d) return;
+    cudaFree(d->arc);
+    cudaFree(d->atoms);
+    cudaFree(d->dq);
+    free(d);
+}
+
+// ---------------------------------------------------------------- decode
+extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *out_dev, uint8_t *out_host,
+                                 size_t out_bytes) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    cudaError_t e;
+    const uint64_t n = r->n_atoms;
+    const uint64_t box_atoms = (uint64_t)r->bnx * r->bny * r->bnz;
+    DecodeJob J;
+    memset(&J, 0, sizeof J);
+    void *p_cnt, *p_off, *p_ent, *p_out, *p_err;
+    if ((e = vcd_scratch(c, VCD_BUF_CNT, (n + 1) * 4 + 16, &p_cnt)) != cudaSuccess ||
+        (e = vcd_scratch(c, VCD_BUF_OFF, (n + 1) * 8, &p_off)) != cudaSuccess ||
+        (e = vcd_scratch(c, VCD_BUF_ENT, r->cap_total * 4 + 16, &p_ent)) != cudaSuccess) {
+        vcd_set_error("decode scratch", e);
+        return vcd_status_of(e);
+    }
+    void *p_ctl;   // [u32 first malformed atom][u32 pad][u64 entries written]
+    if ((e = vcd_scratch(c, VCD_BUF_RED, 64, &p_ctl)) != cudaSuccess) {
+        vcd_set_error("decode scratch", e);
+        return vcd_status_of(e);
+    }
+    p_err = p_ctl;
+    if (out_dev) {
+        p_out = out_dev;
+    } else if ((e = vcd_scratch(c, VCD_BUF_OUT, out_bytes, &p_out)) != cudaSuccess) {
+        vcd_set_error("decode output", e);
+        return vcd_status_of(e);
+    }
+    J.arc = d->arc;
+    J.atoms = d->atoms + r->atom_base;
+    J.acx = r->acx; J.acy = r->acy;
+    J.bax = r->bax; J.bay = r->bay; J.baz = r->baz; J.bnx = r->bnx; J.bny = r->bny;
+    J.n_atoms = n;
+    J.x0 = r->x0; J.y0 = r->y0; J.z0 = r->z0; J.x1 = r->x1; J.y1 = r->y1; J.z1 = r->z1;
+    J.out = (uint8_t *)p_out;
+    J.ox = r->x1 - r->x0; J.oy = r->y1 - r->y0;
+    J.ent = (uint32_t *)p_ent;
+    J.ent_off = (uint64_t *)p_off;
+    J.cnt = (uint32_t *)p_cnt;
+    J.dq = d->dq + r->lod;
+    J.alt_mask = g_dev.tables->alt_mask;
+    J.scan = g_dev.tables->scan;
+    J.err = (uint32_t *)p_err;
+    J.nnz_total = (unsigned long long *)((uint8_t *)p_ctl + 8);
+    memcpy(J.band_start, g_dev.band_start, sizeof J.band_start);
+
+    cudaMemsetAsync(p_ctl, 0, 16, c->stream);
+    cudaMemsetAsync(p_err, 0xFF, 4, c->stream);
+    StageEvents ev;
+    memcpy(ev.ev, c->ev, sizeof ev.ev);
+    launch_decode(J, g_dev.num_sms, c->stream, &ev);
+    uint64_t ctl_h[2] = {0xFFFFFFFFull, 0};
+    cudaMemcpyAsync(ctl_h, p_ctl, 16, cudaMemcpyDeviceToHost, c->stream);
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) {
+        vcd_set_error("decode kernels", e);
+        return vcd_status_of(e);
+    }
+    c->last_ms = vcd_elapsed(ev.ev[0], ev.ev[3]);
+    if (vcd_prof_on()) {
+        const uint64_t nnz = ctl_h[1];
+        vcd_prof_add("decode_place", vcd_elapsed(ev.ev[0], ev.ev[1]), n ? 2 : 0, 24 * n, 8 * n, n);
+        vcd_prof_add("rc_decode", vcd_elapsed(ev.ev[1], ev.ev[2]), n ? 1 : 0, r->payload_bytes + 16 * n, 4 * nnz,
+                     r->present);
+        vcd_prof_add("idct", vcd_elapsed(ev.ev[2], ev.ev[3]), n ? 1 : 0, 4 * nnz + 16 * n, out_bytes, n);
+    }
+    const uint32_t err_h = (uint32_t)ctl_h[0];
+    const uint64_t good = err_h < n ? err_h : n;   // atoms written before the first bad one
+    const int status = (good < box_atoms) ? 1 /*VC_ERR_FORMAT*/ : 0;
+    if (!out_host) return status;
+    if (!status) {
+        if ((e = cudaMemcpyAsync(out_host, p_out, out_bytes, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+            vcd_set_error("decode copy-out", e);
+            return vcd_status_of(e);
+        }
+        return 0;
+    }
+    // error path: only the atoms before the first bad one reach the caller
+    uint8_t *tmp = (uint8_t *)malloc(out_bytes ? out_bytes : 1);
+    if (!tmp) return 3;
+    if ((e = cudaMemcpy(tmp, p_out, out_bytes, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+        free(tmp);
+        vcd_set_error("decode copy-out", e);
+        return vcd_status_of(e);
+    }
+    for (uint64_t t = 0; t < good; ++t) {
+        uint32_t az, ay, ax;
+        box_atom(J, t, az, ay, ax);
+        uint32_t x0 = ax * 32 > r->x0 ? ax * 32 : r->x0, x1 = ax * 32 + 32 < r->x1 ? ax * 32 + 32 : r->x1;
+        uint32_t y0 = ay * 32 > r->y0 ? ay * 32 : r->y0, y1 = ay * 32 + 32 < r->y1 ? ay * 32 + 32 : r->y1;
+        uint32_t z0 = az * 32 > r->z0 ? az * 32 : r->z0, z1 = az * 32 + 32 < r->z1 ? az * 32 + 32 : r->z1;
+        for (uint32_t z = z0; z < z1; ++z)
+            for (uint32_t y = y0; y < y1; ++y) {
+                size_t o = ((size_t)(z - r->z0) * J.oy + (y - r->y0)) * J.ox + (x0 - r->x0);
+                memcpy(out_host + o, tmp + o, x1 - x0);
+            }
+    }
+    free(tmp);
+    return status;
+}

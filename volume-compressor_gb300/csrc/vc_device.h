@@ -1,0 +1,43 @@
+// Private device-runtime state shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "vc_internal.h"
+
+enum {
+    VCD_BUF_CNT = 0, VCD_BUF_OFF, VCD_BUF_ENT, VCD_BUF_OUT,   // decode
+    VCD_BUF_VOL, VCD_BUF_PYR, VCD_BUF_EENT, VCD_BUF_EMETA, VCD_BUF_LEN, VCD_BUF_POS, VCD_BUF_ARC,
+    VCD_BUF_BEST, VCD_BUF_RED,
+    VCD_NBUF
+};
+
+struct vcd_ctx {
+    cudaStream_t stream;
+    void *buf[VCD_NBUF];
+    size_t cap[VCD_NBUF];
+    void *pinned;
+    size_t pinned_cap;
+    cudaEvent_t ev[8];           // stage events of the last call on this thread
+    double last_ms;              // device time of the last decode / encode call (start..end events)
+};
+
+// Kernel statistics, accumulated while profiling is enabled (vcg_profile_enable).
+int vcd_prof_on(void);
+void vcd_prof_add(const char *name, double ms, uint64_t launches, uint64_t bytes_read, uint64_t bytes_written,
+                  uint64_t units);
+float vcd_elapsed(cudaEvent_t a, cudaEvent_t b);
+
+struct vcd_device {
+    int device, num_sms;
+    vcd_tables *tables;          // device copy
+    uint32_t band_start[9];
+};
+
+extern vcd_device g_dev;
+vcd_ctx *vcd_thread_ctx(void);
+cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out);
+cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out);
+void vcd_set_error(const char *what, cudaError_t e);
+int vcd_status_of(cudaError_t e);

@@ -1,0 +1,268 @@
+// Whole-volume encode on the device: LOD pyramid, rate control, canonical
+// placement and archive assembly (the composition vc_encode is defined as in
+// include/vc.h). Host work is limited to the bisection decisions, the 128-byte
+// header and the L1 hash table (a few entries per LOD).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "k_encode.cuh"
+#include "kernels.cuh"
+#include "vc_device.h"
+
+using namespace vcg;
+
+static const uint64_t kChunk = 8192;   // atoms per forward/coder batch (1 GiB of list scratch)
+
+static inline float f_of(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
+static inline uint32_t b_of(float f) { uint32_t b; memcpy(&b, &f, 4); return b; }
+
+#define CK(call, what)                                 \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) {                       \
+            vcd_set_error(what, e_);                   \
+            return vcd_status_of(e_);                  \
+        }                                              \
+    } while (0)
+
+struct EncState {
+    vcd_ctx *c;
+    Layout lay;
+    const uint8_t *lvol[8];
+    uint32_t dims[8][3];
+    uint32_t *ent, *meta, *len, *best;
+    uint64_t *pos;
+    uint8_t *dc, *arc;
+    unsigned long long *red;
+};
+
+// Forward + coder pass over LOD `lod` at `q`: size-only (lengths into len and
+// the totals) or writing payloads into the archive.
+static int run_lod(EncState &S, int lod, float q, bool write) {
+    vcd_quant qc;
+    vch_quant_consts(q, &qc);
+    const uint64_t na = S.lay.base[lod + 1] - S.lay.base[lod];
+    for (uint64_t a0 = 0; a0 < na; a0 += kChunk) {
+        const uint64_t n = na - a0 < kChunk ? na - a0 : kChunk;
+        FwdJob F;
+        F.vol = S.lvol[lod];
+        F.nx = S.dims[lod][0]; F.ny = S.dims[lod][1]; F.nz = S.dims[lod][2];
+        F.acx = S.lay.acx[lod]; F.acy = S.lay.acy[lod];
+        F.first_atom = a0;
+        F.n_atoms = n;
+        F.q = qc;
+        F.rank_base = g_dev.tables->rank_base;
+        F.alt_mask = g_dev.tables->alt_mask;
+        F.ent = S.ent;
+        F.meta = S.meta;
+        const bool prof = vcd_prof_on();
+        if (prof) cudaEventRecord(S.c->ev[4], S.c->stream);
+        launch_fwd(F, g_dev.num_sms, S.c->stream);
+        RcJob R;
+        memset(&R, 0, sizeof R);
+        R.n_atoms = n;
+        R.meta = S.meta;
+        R.ent = S.ent;
+        memcpy(R.band_start, g_dev.band_start, sizeof R.band_start);
+        if (!write) {
+            R.len = S.len + S.lay.base[lod] + a0;
+            R.total_bytes = S.red;
+            R.total_present = S.red + 1;
+        } else {
+            R.arc = S.arc;
+            R.pos = S.pos;
+            R.canon_first = S.lay.base[lod] + a0;
+            R.lay = S.lay;
+            launch_gather_dc(S.meta, n, S.dc + S.lay.base[lod] + a0, S.c->stream);
+        }
+        if (prof) cudaEventRecord(S.c->ev[5], S.c->stream);
+        launch_rc_encode(R, write, S.c->stream);
+        if (prof) {
+            cudaEventRecord(S.c->ev[1], S.c->stream);
+            cudaEventSynchronize(S.c->ev[1]);
+            // forward: volume bytes of the chunk in, coefficient lists out (not counted: scratch)
+            vcd_prof_add("fwd_dct_quant", vcd_elapsed(S.c->ev[4], S.c->ev[5]), 1, n * 32768ull, 0, n);
+            vcd_prof_add(write ? "rc_encode_write" : "rc_encode_size", vcd_elapsed(S.c->ev[5], S.c->ev[1]), 1, 0,
+                         0, n);
+        }
+    }
+    return 0;
+}
+
+extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info, uint8_t **out, size_t *out_len) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    cudaStream_t st = c->stream;
+    EncState S;
+    memset(&S, 0, sizeof S);
+    S.c = c;
+    const int nlod = info->nlod;
+    S.lay.nlod = nlod;
+    uint64_t nvox[8], pyr_bytes = 0, total_atoms = 0;
+    uint32_t d[3] = {info->nx, info->ny, info->nz};
+    for (int l = 0; l < nlod; ++l) {
+        if (l) for (int k = 0; k < 3; ++k) d[k] = (d[k] + 1) / 2;
+        memcpy(S.dims[l], d, sizeof d);
+        nvox[l] = (uint64_t)d[0] * d[1] * d[2];
+        if (l) pyr_bytes += nvox[l];
+        S.lay.acx[l] = (d[0] + 31) / 32; S.lay.acy[l] = (d[1] + 31) / 32; S.lay.acz[l] = (d[2] + 31) / 32;
+        S.lay.base[l] = total_atoms;
+        total_atoms += (uint64_t)S.lay.acx[l] * S.lay.acy[l] * S.lay.acz[l];
+    }
+    S.lay.base[nlod] = total_atoms;
+    for (int l = nlod + 1; l <= 8; ++l) S.lay.base[l] = total_atoms;
+
+    // ---- buffers
+    void *p;
+    if (on_dev) {
+        S.lvol[0] = vol;
+    } else {
+        CK(vcd_scratch(c, VCD_BUF_VOL, nvox[0], &p), "encode volume");
+        CK(cudaMemcpyAsync(p, vol, nvox[0], cudaMemcpyHostToDevice, st), "volume upload");
+        S.lvol[0] = (const uint8_t *)p;
+    }
+    CK(vcd_scratch(c, VCD_BUF_PYR, pyr_bytes + 16, &p), "pyramid");
+    cudaEventRecord(c->ev[6], st);   // device work starts (input already on the device)
+    {
+        uint8_t *q = (uint8_t *)p;
+        for (int l = 1; l < nlod; ++l) {
+            launch_downsample(S.lvol[l - 1], S.dims[l - 1][0], S.dims[l - 1][1], S.dims[l - 1][2], q, g_dev.num_sms, st);
+            S.lvol[l] = q;
+            q += nvox[l];
+        }
+    }
+    CK(vcd_scratch(c, VCD_BUF_EENT, kChunk * VCD_MAX_ENTRIES * 4, &p), "coefficient lists");
+    S.ent = (uint32_t *)p;
+    const uint64_t na0 = S.lay.base[1];
+    // meta (chunk) | len (all atoms) | best LOD0 len | dc (all atoms)
+    size_t meta_b = kChunk * 4, len_b = total_atoms * 4, best_b = na0 * 4, dc_b = total_atoms + 16;
+    CK(vcd_scratch(c, VCD_BUF_EMETA, meta_b + len_b + best_b + dc_b + 64, &p), "encode metadata");
+    S.meta = (uint32_t *)p;
+    S.len = S.meta + kChunk;
+    S.best = S.len + total_atoms;
+    S.dc = (uint8_t *)(S.best + na0);
+    CK(vcd_scratch(c, VCD_BUF_POS, (total_atoms + 1) * 8, &p), "placement");
+    S.pos = (uint64_t *)p;
+    CK(vcd_scratch(c, VCD_BUF_RED, 64, &p), "totals");
+    S.red = (unsigned long long *)p;
+
+    // ---- rate control on LOD0 (bisection over float bit patterns of [0.05, 4096])
+    uint32_t lo = b_of(0.05f), hi = b_of(4096.0f);
+    float best_q = 1.0f;
+    double best_err = INFINITY;
+    uint64_t present = 0, best_bytes = 0;
+    bool have_best = false;
+    for (int it = 0; it < (info->fixed_q ? 0 : 24); ++it) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        float q = f_of(mid);
+        CK(cudaMemsetAsync(S.red, 0, 16, st), "totals reset");
+        run_lod(S, 0, q, false);
+        unsigned long long h[2];
+        CK(cudaMemcpyAsync(h, S.red, 16, cudaMemcpyDeviceToHost, st), "totals read");
+        CK(cudaStreamSynchronize(st), "rate control pass");
+        present = h[1];
+        if (present == 0) break;
+        double ratio = (double)(32768ull * present) / (double)h[0];
+        double err = fabs(ratio - (double)info->target_ratio);
+        if (err < best_err || (err == best_err && q > best_q)) {
+            best_err = err;
+            best_q = q;
+            best_bytes = h[0];
+            have_best = true;
+            CK(cudaMemcpyAsync(S.best, S.len, na0 * 4, cudaMemcpyDeviceToDevice, st), "keep sizes");
+        }
+        if (ratio < (double)info->target_ratio) lo = mid; else hi = mid;
+    }
+    info->q0 = best_q;
+    info->present0 = present;
+    info->bytes0 = best_bytes;
+    float qs[8];
+    if (info->fixed_q) {
+        for (int l = 0; l < nlod; ++l) qs[l] = vch_clamp_q(info->q[l]);
+        info->q0 = qs[0];
+    } else {
+        float q = best_q;
+        for (int l = 0; l < nlod; ++l) { qs[l] = vch_clamp_q(q < 0.05f ? 0.05f : q); q = q * 0.6f; }
+    }
+
+    // ---- sizes of every atom at its LOD's q
+    if (have_best) CK(cudaMemcpyAsync(S.len, S.best, na0 * 4, cudaMemcpyDeviceToDevice, st), "restore sizes");
+    else {
+        CK(cudaMemsetAsync(S.red, 0, 16, st), "totals reset");
+        run_lod(S, 0, qs[0], false);
+    }
+    for (int l = 1; l < nlod; ++l) run_lod(S, l, qs[l], false);
+
+    // ---- canonical placement: exclusive scan of consumed bytes
+    const uint64_t head = 128 + 16 * info->l1_cap;
+    PlaceJob P;
+    P.n_total = total_atoms;
+    P.pos = S.pos;
+    P.len = S.len;
+    P.dc = S.dc;
+    P.lay = S.lay;
+    launch_consume(P, st);
+    launch_scan_u64(S.pos, total_atoms, head, S.pos + total_atoms, st);
+    uint64_t *pos_h = (uint64_t *)malloc((total_atoms + 1) * 8);
+    if (!pos_h) return 3;
+    cudaError_t e = cudaMemcpyAsync(pos_h, S.pos, (total_atoms + 1) * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { free(pos_h); vcd_set_error("placement", e); return vcd_status_of(e); }
+    const uint64_t total = pos_h[total_atoms];
+
+    // ---- archive: zeroed, payloads + slots on the device, head on the host
+    e = vcd_scratch(c, VCD_BUF_ARC, total + 16, &p);
+    if (e != cudaSuccess) { free(pos_h); vcd_set_error("archive buffer", e); return vcd_status_of(e); }
+    S.arc = (uint8_t *)p;
+    P.arc = S.arc;
+    cudaMemsetAsync(S.arc, 0, total, st);
+    for (int l = 0; l < nlod; ++l) run_lod(S, l, qs[l], true);
+    launch_slots(P, st);
+    cudaEventRecord(c->ev[7], st);   // device work ends (the archive head and copy-out follow)
+
+    uint8_t *hd = (uint8_t *)calloc(head, 1);
+    if (!hd) { free(pos_h); return 3; }
+    uint32_t w32[9] = {0x00314356u, 1u, 32u, 1u, 32u, (uint32_t)nlod, info->nx, info->ny, info->nz};
+    memcpy(hd, w32, sizeof w32);
+    memcpy(hd + 36, &info->target_ratio, 4);
+    uint64_t regions = 0;
+    const uint64_t mask = info->l1_cap - 1;
+    for (int l = 0; l < nlod; ++l) {   // regions in creation order (raster of regions)
+        uint32_t nrx = (S.lay.acx[l] + 31) / 32, nry = (S.lay.acy[l] + 31) / 32, nrz = (S.lay.acz[l] + 31) / 32;
+        for (uint32_t rz = 0; rz < nrz; ++rz)
+            for (uint32_t ry = 0; ry < nry; ++ry)
+                for (uint32_t rx = 0; rx < nrx; ++rx) {
+                    uint64_t key = vch_region_key(l, rz, ry, rx);
+                    uint64_t blk = pos_h[S.lay.region_first(l, rz * 32, ry * 32, rx * 32)];
+                    uint64_t i = vch_mix64(key) & mask;
+                    while (1) {
+                        uint64_t bref;
+                        memcpy(&bref, hd + 128 + i * 16 + 8, 8);
+                        if (!bref) break;
+                        i = (i + 1) & mask;
+                    }
+                    memcpy(hd + 128 + i * 16, &key, 8);
+                    memcpy(hd + 128 + i * 16 + 8, &blk, 8);
+                    ++regions;
+                }
+    }
+    uint64_t h64[4] = {info->l1_cap, regions, 128, total};
+    memcpy(hd + 40, h64, sizeof h64);
+    for (int l = 0; l < nlod; ++l) memcpy(hd + 72 + 4 * l, &qs[l], 4);
+    free(pos_h);
+    e = cudaMemcpyAsync(S.arc, hd, head, cudaMemcpyHostToDevice, st);
+    uint8_t *res = (uint8_t *)malloc(total);
+    if (!res) { cudaStreamSynchronize(st); free(hd); return 3; }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(res, S.arc, total, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    free(hd);
+    if (e != cudaSuccess) { free(res); vcd_set_error("archive assembly", e); return vcd_status_of(e); }
+    c->last_ms = vcd_elapsed(c->ev[6], c->ev[7]);
+    *out = res;
+    *out_len = total;
+    return 0;
+}

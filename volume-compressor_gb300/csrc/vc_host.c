@@ -1,0 +1,506 @@
+// Host half of the GB300 volume codec: the vc.h API, archive header parsing and
+// validation, atom resolution through the v1 hash index / v2 directory, and the
+// small per-q tables the kernels consume. All voxel work (encode and decode)
+// is delegated to the CUDA device layer through vc_internal.h; nothing here
+// decodes or encodes an atom.
+#include <math.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/vc.h"
+#include "vc_internal.h"
+#include "vc_release_tables.h"
+
+#define VC_API __attribute__((visibility("default")))
+
+// ---------------------------------------------------------------------------
+// Archive format constants (src/vc/vc.c:567-575, 660-718)
+// ---------------------------------------------------------------------------
+#define FILE_HDR 128u
+#define MAGIC 0x00314356u
+#define R_ATOMS 32u
+#define L2_BYTES (32768ull * 16ull)
+#define NO_OFFSET 0xFFFFFFFFFFFFFFFFull
+#define ZERO_REGION 1ull
+
+static void (*g_hook)(const char *) = NULL;
+VC_API void vc_set_panic_hook(void (*hook)(const char *)) { g_hook = hook; }
+VC_API uint32_t vc_region_atoms(void) { return R_ATOMS; }
+
+static void report(const char *fmt, ...) {
+    char msg[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    if (g_hook) g_hook(msg);
+    fprintf(stderr, "vc: %s\n", msg);
+}
+
+static inline uint32_t rd32(const uint8_t *p) { uint32_t v; memcpy(&v, p, 4); return v; }
+static inline uint64_t rd64(const uint8_t *p) { uint64_t v; memcpy(&v, p, 8); return v; }
+static inline float f_of(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
+static inline uint32_t b_of(float f) { uint32_t b; memcpy(&b, &f, 4); return b; }
+
+// src/vc/vc.c:721-730
+uint64_t vch_mix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+uint64_t vch_region_key(int lod, uint32_t rz, uint32_t ry, uint32_t rx) {
+    return ((uint64_t)(lod & 7) << 45) | ((uint64_t)(rz & 0x7FFF) << 30) |
+           ((uint64_t)(ry & 0x7FFF) << 15) | (uint64_t)(rx & 0x7FFF);
+}
+
+static vc_dims lod_dims_of(vc_dims d, int lod) {   // src/vc/vc.c:733-739
+    for (int i = 0; i < lod; ++i) { d.nx = (d.nx + 1) / 2; d.ny = (d.ny + 1) / 2; d.nz = (d.nz + 1) / 2; }
+    return d;
+}
+static void region_grid(vc_dims d0, int lod, uint32_t *nrz, uint32_t *nry, uint32_t *nrx) {
+    vc_dims d = lod_dims_of(d0, lod);
+    *nrx = ((d.nx + 31) / 32 + R_ATOMS - 1) / R_ATOMS;
+    *nry = ((d.ny + 31) / 32 + R_ATOMS - 1) / R_ATOMS;
+    *nrz = ((d.nz + 31) / 32 + R_ATOMS - 1) / R_ATOMS;
+}
+static int dims_valid(vc_dims d) {
+    return d.nx && d.ny && d.nz && d.nx <= VC_MAX_DIM && d.ny <= VC_MAX_DIM && d.nz <= VC_MAX_DIM;
+}
+
+// ---------------------------------------------------------------------------
+// Per-q tables. The quantiser step of raster index i is base_q * g_step[i]; the
+// release build's g_step holds one of two floats per frequency (step class =
+// f + 94*alt). These helpers evaluate exactly the float operations of the
+// reference's release build (compiled with -ffp-contract=off).
+// ---------------------------------------------------------------------------
+static float class_g(int cls) {
+    int f = cls % 94, alt = cls / 94;
+    return f_of(alt ? vc_step_alt_bits[f] : vc_step_base_bits[f]);
+}
+
+// RCPPS estimate: a function of the top 11 mantissa bits, scaled by the exponent.
+static float rcp_est(float x) {
+    uint32_t b = b_of(x), e = (b >> 23) & 0xFFu, r = vc_rcp_est_bits[(b >> 12) & 0x7FFu];
+    uint32_t re = ((r >> 23) & 0xFFu) - (e - 127u);
+    return f_of((b & 0x80000000u) | (re << 23) | (r & 0x7FFFFFu));
+}
+
+void vch_quant_consts(float base_q, vcd_quant *q) {
+    for (int c = 0; c < VCD_NCLASS; ++c) {
+        float step = base_q * class_g(c);
+        float r = rcp_est(step);
+        q->step[c] = step;
+        q->dz[c] = 0.8f * step;
+        q->rr[c] = (r + r) - r * (r * step);
+    }
+}
+
+void vch_dq_consts(float base_q, vcd_dq *dq) {   // src/vc/vc.c:318-326
+    const float c = (0.4f - 1.0f) + 0.8f;
+    for (int k = 0; k < VCD_NCLASS; ++k) {
+        float step = base_q * class_g(k);
+        dq->step[k] = (int32_t)lrintf(step * 256.0f);
+        dq->bias[k] = (int32_t)lrintf(c * step * 256.0f);
+    }
+}
+
+float vch_clamp_q(float q) {   // src/vc/vc.c:1072-1073
+    if (q < 0.05f) q = 0.05f;
+    if (q > 4096.0f) q = 4096.0f;
+    return q;
+}
+
+static uint32_t n2(int s) { return (s < 0 || s > 62) ? 0u : (uint32_t)((s < 62 - s ? s : 62 - s) + 1); }
+
+void vch_tables(vcd_tables *t) {
+    memcpy(t->alt_mask, vc_step_alt_mask, sizeof t->alt_mask);
+    // scan order: ascending L1 frequency, ties by raster index (src/vc/vc.c:258-288)
+    uint32_t first[95] = {0};
+    for (uint32_t r = 0; r < 32768; ++r) first[(r >> 10) + ((r >> 5) & 31) + (r & 31) + 1]++;
+    for (int f = 1; f <= 94; ++f) first[f] += first[f - 1];
+    uint32_t fill[94];
+    memcpy(fill, first, sizeof fill);
+    for (uint32_t r = 0; r < 32768; ++r) t->scan[fill[(r >> 10) + ((r >> 5) & 31) + (r & 31)]++] = (uint16_t)r;
+    // rank_base[f][kz]: scan position of the first index with frequency f and
+    // plane kz (the one with the smallest valid ky)
+    for (int f = 0; f < 94; ++f) {
+        uint32_t acc = first[f];
+        for (int kz = 0; kz < 32; ++kz) {
+            t->rank_base[f * 32 + kz] = (uint16_t)(acc > 65535 ? 65535 : acc);
+            acc += n2(f - kz);
+        }
+    }
+    // significance band b holds frequencies [12b, 12b+11] (b = 7: >= 84) (src/vc/vc.c:462-468)
+    for (int b = 0; b < 8; ++b) t->band_start[b] = first[12 * b];
+    t->band_start[8] = 32768;
+}
+
+// ---------------------------------------------------------------------------
+// Reader (src/vc/vc.c:1250-1555)
+// ---------------------------------------------------------------------------
+struct vc_archive {
+    const uint8_t *buf;
+    size_t len;
+    vc_dims d0;
+    int nlod, version;
+    uint64_t l1_off, l1_cap, dir_off, region_prefix[VC_NLOD + 1];
+    float base_q[VC_NLOD];
+    // device residency, built on first decode
+    pthread_mutex_t mu;
+    int resident;           // 0 not yet, 1 ok, -1 failed
+    vcd_atom *atoms;        // all LODs, LOD-major, raster (az, ay, ax) within a LOD
+    uint64_t lod_base[VC_NLOD + 1];
+    vcd_archive *dev;
+};
+
+static int parse_header(vc_archive *a, const uint8_t *h, uint64_t len) {   // src/vc/vc.c:1285-1314
+    if (rd32(h + 0) != MAGIC || rd32(h + 8) != 32 || rd32(h + 16) != R_ATOMS) return -1;
+    uint32_t ver = rd32(h + 4), nlod = rd32(h + 20);
+    if (nlod == 0 || nlod > VC_NLOD) return -1;
+    a->len = len;
+    a->nlod = (int)nlod;
+    a->d0.nx = rd32(h + 24); a->d0.ny = rd32(h + 28); a->d0.nz = rd32(h + 32);
+    for (int l = 0; l < VC_NLOD; ++l) a->base_q[l] = f_of(rd32(h + 72 + 4 * l));
+    if (ver == 2) {
+        a->version = 2;
+        a->dir_off = rd64(h + 40);
+        uint64_t cnt = rd64(h + 48), acc = 0;
+        if (a->dir_off > len || cnt > (len - a->dir_off) / 16) return -1;
+        for (int l = 0; l < a->nlod; ++l) {
+            a->region_prefix[l] = acc;
+            uint32_t z, y, x;
+            region_grid(a->d0, l, &z, &y, &x);
+            acc += (uint64_t)z * y * x;
+        }
+        a->region_prefix[a->nlod] = acc;
+        return acc == cnt ? 0 : -1;
+    }
+    if (ver != 1 || rd32(h + 12) != 1) return -1;
+    a->version = 1;
+    a->l1_off = rd64(h + 56);
+    a->l1_cap = rd64(h + 40);
+    if (!a->l1_cap || (a->l1_cap & (a->l1_cap - 1))) return -1;
+    if (a->l1_off > len || a->l1_cap > (len - a->l1_off) / 16) return -1;
+    return 0;
+}
+
+VC_API vc_archive *vc_open(const uint8_t *archive, size_t len) {
+    if (!archive || len < FILE_HDR) return NULL;
+    vc_archive *a = (vc_archive *)calloc(1, sizeof *a);
+    if (!a) return NULL;
+    a->buf = archive;
+    if (parse_header(a, archive, len) != 0) { free(a); return NULL; }
+    pthread_mutex_init(&a->mu, NULL);
+    return a;
+}
+
+VC_API void vc_close(vc_archive *a) {
+    if (!a) return;
+    if (a->dev) vcd_free_archive(a->dev);
+    free(a->atoms);
+    pthread_mutex_destroy(&a->mu);
+    free(a);
+}
+
+VC_API int vc_archive_version(const vc_archive *a) { return a ? a->version : 0; }
+
+VC_API vc_status vc_lod_dims(const vc_archive *a, int lod, vc_dims *out) {
+    if (!a || lod < 0 || lod >= a->nlod || !out) return VC_ERR_RANGE;
+    *out = lod_dims_of(a->d0, lod);
+    return VC_OK;
+}
+
+// L2 block of a region: 0 absent, ZERO_REGION, or a block offset that lies in
+// the file. The v1 probe is bounded by the table size (the reference loops
+// forever on a full table without the key; src/vc/vc.c:1349-1360).
+static uint64_t region_block(const vc_archive *a, int lod, uint32_t rz, uint32_t ry, uint32_t rx) {
+    uint64_t blk;
+    if (a->version == 2) {
+        uint32_t nrz, nry, nrx;
+        region_grid(a->d0, lod, &nrz, &nry, &nrx);
+        if (rz >= nrz || ry >= nry || rx >= nrx) return 0;
+        uint64_t ri = a->region_prefix[lod] + ((uint64_t)rz * nry + ry) * nrx + rx;
+        if (ri >= a->region_prefix[a->nlod]) return 0;
+        const uint8_t *e = a->buf + a->dir_off + ri * 16;
+        uint32_t fl = rd32(e + 12);
+        if (fl == 0) return 0;
+        if (fl == 1) return ZERO_REGION;
+        blk = rd64(e);
+    } else {
+        uint64_t key = vch_region_key(lod, rz, ry, rx), mask = a->l1_cap - 1, i = vch_mix64(key) & mask;
+        for (uint64_t step = 0;; ++step) {
+            if (step >= a->l1_cap) return 0;
+            const uint8_t *e = a->buf + a->l1_off + i * 16;
+            uint64_t bref = rd64(e + 8);
+            if (!bref) return 0;
+            if (rd64(e) == key) { blk = bref; break; }
+            i = (i + 1) & mask;
+        }
+        if (blk == ZERO_REGION) return ZERO_REGION;
+    }
+    if (blk > a->len || L2_BYTES > a->len - blk) return 0;   // corrupt guard (src/vc/vc.c:1389,1400)
+    return blk;
+}
+
+// slot flags of an atom given its region's block (src/vc/vc.c:1365-1373)
+static int slot_of(const vc_archive *a, uint64_t blk, uint32_t az, uint32_t ay, uint32_t ax,
+                   uint64_t *off, uint32_t *len, uint8_t *dc) {
+    if (blk == 0) return 0;
+    if (blk == ZERO_REGION) return 2;
+    const uint8_t *s = a->buf + blk + ((((uint64_t)(az & 31) * 32 + (ay & 31)) * 32 + (ax & 31)) * 16);
+    uint8_t fl = s[12];
+    if (fl == 1) { *off = rd64(s); *len = rd32(s + 8); *dc = s[13]; }
+    return fl;
+}
+
+static int resolve(const vc_archive *a, int lod, uint32_t az, uint32_t ay, uint32_t ax,
+                   uint64_t *off, uint32_t *len, uint8_t *dc) {
+    return slot_of(a, region_block(a, lod, az / 32, ay / 32, ax / 32), az, ay, ax, off, len, dc);
+}
+
+VC_API vc_cover vc_atom_coverage(const vc_archive *a, int lod, uint32_t az, uint32_t ay, uint32_t ax) {
+    if (!a || lod < 0 || lod >= a->nlod) return VC_ABSENT;
+    uint64_t off; uint32_t len; uint8_t dc;
+    int fl = resolve(a, lod, az, ay, ax, &off, &len, &dc);
+    return fl == 1 ? VC_PRESENT : fl == 2 ? VC_KNOWN_ZERO : VC_ABSENT;
+}
+
+VC_API vc_cover vc_atom_payload_range(const vc_archive *a, int lod, uint32_t az, uint32_t ay, uint32_t ax,
+                                      uint64_t *off, uint32_t *len) {
+    if (off) *off = 0;
+    if (len) *len = 0;
+    if (!a || lod < 0 || lod >= a->nlod) return VC_ABSENT;
+    uint64_t o = 0; uint32_t l = 0; uint8_t dc = 0;
+    int fl = resolve(a, lod, az, ay, ax, &o, &l, &dc);
+    if (fl == 1) { if (off) *off = o; if (len) *len = l; return VC_PRESENT; }
+    return fl == 2 ? VC_KNOWN_ZERO : VC_ABSENT;
+}
+
+VC_API vc_cover vc_region_blob_range(const vc_archive *a, int lod, uint32_t rz, uint32_t ry, uint32_t rx,
+                                     uint64_t *off, uint64_t *len) {   // src/vc/vc.c:1455-1471
+    if (off) *off = 0;
+    if (len) *len = 0;
+    if (!a || a->version != 2 || lod < 0 || lod >= a->nlod) return VC_ABSENT;
+    uint32_t nrz, nry, nrx;
+    region_grid(a->d0, lod, &nrz, &nry, &nrx);
+    if (rz >= nrz || ry >= nry || rx >= nrx) return VC_ABSENT;
+    uint64_t ri = a->region_prefix[lod] + ((uint64_t)rz * nry + ry) * nrx + rx;
+    if (ri >= a->region_prefix[a->nlod]) return VC_ABSENT;
+    const uint8_t *e = a->buf + a->dir_off + ri * 16;
+    uint32_t fl = rd32(e + 12);
+    if (fl == 1) return VC_KNOWN_ZERO;
+    if (fl != 2) return VC_ABSENT;
+    if (off) *off = rd64(e);
+    if (len) *len = rd32(e + 8);
+    return VC_PRESENT;
+}
+
+// Resolve every atom of every LOD once, validate payload ranges, and move the
+// archive bytes plus the table into device memory.
+static int make_resident(vc_archive *a) {
+    pthread_mutex_lock(&a->mu);
+    if (a->resident) { int r = a->resident; pthread_mutex_unlock(&a->mu); return r > 0 ? 0 : -1; }
+    int rc = -1;
+    if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); goto done; }
+    uint64_t total = 0;
+    for (int l = 0; l < a->nlod; ++l) {
+        vc_dims d = lod_dims_of(a->d0, l);
+        a->lod_base[l] = total;
+        total += (uint64_t)((d.nx + 31) / 32) * ((d.ny + 31) / 32) * ((d.nz + 31) / 32);
+    }
+    a->lod_base[a->nlod] = total;
+    a->atoms = (vcd_atom *)calloc(total ? total : 1, sizeof(vcd_atom));
+    if (!a->atoms) goto done;
+    vcd_dq dq[VC_NLOD];
+    for (int l = 0; l < a->nlod; ++l) {
+        vc_dims d = lod_dims_of(a->d0, l);
+        uint32_t acx = (d.nx + 31) / 32, acy = (d.ny + 31) / 32, acz = (d.nz + 31) / 32;
+        vch_dq_consts(a->base_q[l], &dq[l]);
+        for (uint32_t rz = 0; rz * 32 < acz; ++rz)
+            for (uint32_t ry = 0; ry * 32 < acy; ++ry)
+                for (uint32_t rx = 0; rx * 32 < acx; ++rx) {
+                    uint64_t blk = region_block(a, l, rz, ry, rx);
+                    for (uint32_t az = rz * 32; az < acz && az < rz * 32 + 32; ++az)
+                        for (uint32_t ay = ry * 32; ay < acy && ay < ry * 32 + 32; ++ay)
+                            for (uint32_t ax = rx * 32; ax < acx && ax < rx * 32 + 32; ++ax) {
+                                uint64_t off = 0; uint32_t len = 0; uint8_t dc = 0;
+                                vcd_atom *t = &a->atoms[a->lod_base[l] + ((uint64_t)az * acy + ay) * acx + ax];
+                                int fl = slot_of(a, blk, az, ay, ax, &off, &len, &dc);
+                                if (fl != 1) { t->kind = VCD_EMPTY; continue; }
+                                // src/vc/vc.c:1413, without the wrap-around of off + len
+                                if (off == NO_OFFSET || len < 1 || off > a->len || len > a->len - off) {
+                                    t->kind = VCD_BAD;
+                                    continue;
+                                }
+                                t->kind = VCD_PRESENT; t->off = off; t->len = len; t->dc = dc;
+                            }
+                }
+    }
+    if (vcd_upload_archive(&a->dev, a->buf, a->len, a->atoms, total, dq, a->nlod) != 0) {
+        report("archive upload failed: %s", vcd_last_error());
+        goto done;
+    }
+    rc = 0;
+done:
+    a->resident = rc == 0 ? 1 : -1;
+    pthread_mutex_unlock(&a->mu);
+    return rc;
+}
+
+// Entry capacity of one atom's coefficient list: every nonzero level spends a
+// whole bypass (sign) bit, so a stream of n range-coder bytes cannot carry more
+// than 8n of them; hostile streams that would exceed it are decoded on a slow
+// path inside the kernel.
+static inline uint64_t entry_cap(const vcd_atom *t) {
+    uint64_t c = 8ull * (t->len - 1) + 64;
+    return c > VCD_MAX_ENTRIES ? VCD_MAX_ENTRIES : c;
+}
+
+// Shared by decode_region / decode_atom / decode_lod: out_dev (device) or out
+// (host) receives the box raster.
+static vc_status decode_box(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev) {
+    if (make_resident(a) != 0) return VC_ERR_IO;
+    vc_dims d = lod_dims_of(a->d0, lod);
+    vcd_region r;
+    memset(&r, 0, sizeof r);
+    r.lod = lod;
+    r.atoms = a->atoms + a->lod_base[lod];
+    r.atom_base = a->lod_base[lod];
+    r.acx = (d.nx + 31) / 32; r.acy = (d.ny + 31) / 32; r.acz = (d.nz + 31) / 32;
+    r.x0 = b.x0; r.y0 = b.y0; r.z0 = b.z0; r.x1 = b.x1; r.y1 = b.y1; r.z1 = b.z1;
+    r.bax = b.x0 / 32; r.bay = b.y0 / 32; r.baz = b.z0 / 32;
+    r.bnx = (b.x1 - 1) / 32 - r.bax + 1; r.bny = (b.y1 - 1) / 32 - r.bay + 1; r.bnz = (b.z1 - 1) / 32 - r.baz + 1;
+    uint64_t n = (uint64_t)r.bnx * r.bny * r.bnz, cap = 0, i = 0, pay = 0, present = 0;
+    vc_status st = VC_OK;
+    for (uint32_t z = 0; z < r.bnz && st == VC_OK; ++z)
+        for (uint32_t y = 0; y < r.bny && st == VC_OK; ++y)
+            for (uint32_t x = 0; x < r.bnx; ++x, ++i) {
+                const vcd_atom *t = &r.atoms[((uint64_t)(r.baz + z) * r.acy + (r.bay + y)) * r.acx + r.bax + x];
+                if (t->kind == VCD_BAD) { st = VC_ERR_FORMAT; break; }
+                if (t->kind == VCD_PRESENT) { cap += entry_cap(t); pay += t->len; ++present; }
+            }
+    r.n_atoms = st == VC_OK ? n : i;
+    r.cap_total = cap;
+    r.payload_bytes = pay;
+    r.present = present;
+    size_t bytes = (size_t)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
+    int rc = vcd_decode_region(a->dev, &r, out_dev, out, bytes);
+    if (rc == VC_ERR_FORMAT || st == VC_ERR_FORMAT) return VC_ERR_FORMAT;
+    if (rc) report("decode failed: %s", vcd_last_error());
+    return (vc_status)rc;
+}
+
+VC_API vc_status vc_decode_region(vc_archive *a, int lod, vc_box b, uint8_t *out) {
+    if (!a || lod < 0 || lod >= a->nlod || !out) return VC_ERR_RANGE;
+    vc_dims d = lod_dims_of(a->d0, lod);
+    if (b.x1 > d.nx || b.y1 > d.ny || b.z1 > d.nz) return VC_ERR_RANGE;
+    if (b.x0 >= b.x1 || b.y0 >= b.y1 || b.z0 >= b.z1) return VC_ERR_RANGE;
+    return decode_box(a, lod, b, out, NULL);
+}
+
+VC_API vc_status vc_decode_atom(vc_archive *a, int lod, int ax, int ay, int az, uint8_t out[VC_ATOM3]) {
+    if (!a || lod < 0 || lod >= a->nlod || !out) return VC_ERR_RANGE;
+    vc_dims d = lod_dims_of(a->d0, lod);
+    if ((uint32_t)ax >= (d.nx + 31) / 32 || (uint32_t)ay >= (d.ny + 31) / 32 || (uint32_t)az >= (d.nz + 31) / 32)
+        return VC_ERR_RANGE;
+    vc_box b = {(uint32_t)ax * 32, (uint32_t)ay * 32, (uint32_t)az * 32,
+                (uint32_t)ax * 32 + 32, (uint32_t)ay * 32 + 32, (uint32_t)az * 32 + 32};
+    vc_status s = decode_box(a, lod, b, out, NULL);
+    if (s == VC_ERR_FORMAT) memset(out, 0, VC_ATOM3);
+    return s;
+}
+
+VC_API vc_status vc_decode_lod(vc_archive *a, int lod, uint8_t *out_vol, vc_dims *out_dims) {
+    vc_dims d;
+    vc_status s = vc_lod_dims(a, lod, &d);
+    if (s != VC_OK) return s;
+    if (out_dims) *out_dims = d;
+    vc_box b = {0, 0, 0, d.nx, d.ny, d.nz};
+    return vc_decode_region(a, lod, b, out_vol);
+}
+
+// Device-output variants (include/vcg.h).
+VC_API vc_status vcg_decode_region_device(vc_archive *a, int lod, vc_box b, uint8_t *out_dev) {
+    if (!a || lod < 0 || lod >= a->nlod || !out_dev) return VC_ERR_RANGE;
+    vc_dims d = lod_dims_of(a->d0, lod);
+    if (b.x1 > d.nx || b.y1 > d.ny || b.z1 > d.nz) return VC_ERR_RANGE;
+    if (b.x0 >= b.x1 || b.y0 >= b.y1 || b.z0 >= b.z1) return VC_ERR_RANGE;
+    return decode_box(a, lod, b, NULL, out_dev);
+}
+
+VC_API vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev, vc_dims *out_dims) {
+    vc_dims d;
+    vc_status s = vc_lod_dims(a, lod, &d);
+    if (s != VC_OK) return s;
+    if (out_dims) *out_dims = d;
+    vc_box b = {0, 0, 0, d.nx, d.ny, d.nz};
+    return vcg_decode_region_device(a, lod, b, out_dev);
+}
+
+VC_API vc_status vcg_make_resident(vc_archive *a) {
+    if (!a) return VC_ERR_RANGE;
+    return make_resident(a) == 0 ? VC_OK : VC_ERR_IO;
+}
+
+// ---------------------------------------------------------------------------
+// Encode (the canonical vc_encode composition, see include/vc.h)
+// ---------------------------------------------------------------------------
+static int nlod_for(vc_dims d0) {   // src/vc/vc.c:1001-1006
+    int nlod = 1;
+    for (int l = 1; l < VC_NLOD; ++l) {
+        vc_dims d = lod_dims_of(d0, l);
+        nlod = l + 1;
+        if (d.nx <= 1 && d.ny <= 1 && d.nz <= 1) break;
+    }
+    return nlod;
+}
+
+static vc_status encode_common(const uint8_t *vol, int on_device, vc_dims dims, float target,
+                               const float *fixed_q, uint8_t **out, size_t *out_len, float *q0) {
+    if (!vol || !out || !out_len || !dims_valid(dims) || !(target >= 1.0f)) return VC_ERR_RANGE;
+    if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); return VC_ERR_IO; }
+    vcd_encode_info info;
+    memset(&info, 0, sizeof info);
+    info.nx = dims.nx; info.ny = dims.ny; info.nz = dims.nz;
+    info.target_ratio = target;
+    info.nlod = nlod_for(dims);
+    if (fixed_q) {
+        info.fixed_q = 1;
+        for (int l = 0; l < info.nlod; ++l) {
+            if (!(fixed_q[l] > 0.0f)) return VC_ERR_RANGE;   // vc_append_atom needs a q (src/vc/vc.c:1100)
+            info.q[l] = fixed_q[l];
+        }
+    }
+    uint64_t max_regions = 0;   // src/vc/vc.c:1012-1021
+    for (int l = 0; l < info.nlod; ++l) {
+        uint32_t z, y, x;
+        region_grid(dims, l, &z, &y, &x);
+        max_regions += (uint64_t)z * y * x;
+    }
+    info.l1_cap = 1024;
+    while (info.l1_cap < max_regions * 2) info.l1_cap <<= 1;
+    int rc = vcd_encode(vol, on_device, &info, out, out_len);
+    if (rc) { report("encode failed: %s", vcd_last_error()); return (vc_status)rc; }
+    if (q0) *q0 = info.q0;
+    return VC_OK;
+}
+
+VC_API vc_status vc_encode(const uint8_t *vol, vc_dims dims, float target_ratio, uint8_t **out_archive,
+                           size_t *out_len) {
+    return encode_common(vol, 0, dims, target_ratio, NULL, out_archive, out_len, NULL);
+}
+
+VC_API vc_status vcg_encode_device(const uint8_t *vol_dev, vc_dims dims, float target_ratio,
+                                   uint8_t **out_archive, size_t *out_len, float *q0) {
+    return encode_common(vol_dev, 1, dims, target_ratio, NULL, out_archive, out_len, q0);
+}
+
+VC_API vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
+                              const float base_q[VC_NLOD], uint8_t **out_archive, size_t *out_len) {
+    if (!base_q) return VC_ERR_RANGE;
+    return encode_common(vol, vol_on_device, dims, target_ratio, base_q, out_archive, out_len, NULL);
+}

@@ -1,0 +1,106 @@
+// Internal interface between the C host library (vc_host.c) and the CUDA
+// device layer (*.cu): plain C structs and extern "C" functions, no CUDA or
+// torch types. Not installed; the public boundary is include/vc.h + vcg.h.
+#ifndef VC_INTERNAL_H
+#define VC_INTERNAL_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VCD_NCLASS 188          // quantizer step classes: L1 frequency f (0..93) + 94 * alt bit
+#define VCD_MAX_ENTRIES 32768u  // one atom's coefficients
+
+// Kinds in the resolved atom table.
+enum { VCD_EMPTY = 0, VCD_PRESENT = 1, VCD_BAD = 2 };
+
+// One atom of an archive, resolved on the host from the v1 hash index / v2
+// directory plus its L2 slot (src/vc/vc.c:1349-1402), with the payload range
+// already checked against the archive length.
+typedef struct {
+    uint64_t off;   // payload byte offset in the archive (PRESENT)
+    uint32_t len;   // payload bytes, >= 1 (PRESENT)
+    uint8_t kind;   // VCD_EMPTY (absent or known-zero), VCD_PRESENT, VCD_BAD
+    uint8_t dc;     // slot dc byte (informational; decode uses payload byte 0)
+    uint16_t rsv;
+} vcd_atom;
+
+// Per-LOD dequantisation tables by step class (src/vc/vc.c:314-326).
+typedef struct {
+    int32_t step[VCD_NCLASS];
+    int32_t bias[VCD_NCLASS];
+} vcd_dq;
+
+// Per-q quantiser constants by step class (src/vc/vc.c:293-306 as the release
+// build evaluates it): step, dead zone 0.8*step, refined reciprocal of step.
+typedef struct {
+    float step[VCD_NCLASS];
+    float dz[VCD_NCLASS];
+    float rr[VCD_NCLASS];
+} vcd_quant;
+
+// Constant tables shared by every kernel.
+typedef struct {
+    uint32_t alt_mask[1024];   // bit i: raster index i uses the alternate step value
+    uint16_t scan[32768];      // scan position -> raster index
+    uint16_t rank_base[94 * 32];  // scan position of (f, kz, ky = max(0, f-kz-31))
+    uint32_t band_start[9];    // first scan position of each significance band, [8] = 32768
+} vcd_tables;
+
+// Region / LOD decode request, resolved on the host.
+typedef struct {
+    const vcd_atom *atoms;      // host table of this LOD (raster az, ay, ax)
+    uint64_t atom_base;         // index of this LOD's first atom in the device table
+    uint32_t acx, acy, acz;     // LOD atom grid
+    uint32_t x0, y0, z0, x1, y1, z1;   // box (voxels)
+    uint32_t bax, bay, baz;     // first atom of the box
+    uint32_t bnx, bny, bnz;     // atoms of the box per axis
+    uint64_t n_atoms;           // atoms to decode (box order z, y, x), stops at the first bad
+    uint64_t cap_total;         // sum of entry capacities of those atoms
+    uint64_t payload_bytes;     // sum of their payload lengths (for profiling)
+    uint64_t present;           // PRESENT atoms among them
+    int lod;
+} vcd_region;
+
+typedef struct vcd_archive vcd_archive;   // device residency of one archive
+
+// ---- device layer (vc_device.cu) ------------------------------------------
+int  vcd_init(void);                        // 0 ok; -1 no usable device
+const char *vcd_last_error(void);
+int  vcd_upload_archive(vcd_archive **out, const uint8_t *buf, size_t len, const vcd_atom *atoms,
+                        uint64_t n_atoms, const vcd_dq *dq /*nlod*/, int nlod);
+void vcd_free_archive(vcd_archive *d);
+// decode into a device buffer (out_dev, box bytes) or, when out_dev is NULL, into
+// the host buffer out_host (box raster); returns 0 or a vc_status
+int  vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *out_dev, uint8_t *out_host,
+                       size_t out_bytes);
+
+// Encode: volume (device or host) -> canonical archive (host malloc).
+typedef struct {
+    uint32_t nx, ny, nz;
+    float target_ratio;
+    int nlod;
+    uint64_t l1_cap;
+    int fixed_q;        // 1: use q[] as given (no rate control)
+    float q[8];         // per-LOD base_q when fixed_q
+    float q0;           // chosen LOD0 base_q (output)
+    uint64_t present0;  // present LOD0 atoms (output)
+    uint64_t bytes0;    // LOD0 payload bytes at q0 (output)
+} vcd_encode_info;
+int  vcd_encode(const uint8_t *vol, int vol_on_device, vcd_encode_info *info, uint8_t **out,
+                size_t *out_len);
+
+// ---- host helpers shared with the device layer (vc_host.c) ----------------
+void vch_tables(vcd_tables *t);
+void vch_quant_consts(float base_q, vcd_quant *q);
+void vch_dq_consts(float base_q, vcd_dq *dq);
+float vch_clamp_q(float q);
+uint64_t vch_region_key(int lod, uint32_t rz, uint32_t ry, uint32_t rx);
+uint64_t vch_mix64(uint64_t x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,332 @@
+"""Python binding (ctypes) of the GB300 volume codec's C ABI (include/vc.h,
+include/vcg.h) and of the host synthetic-volume generator.
+
+The library is the in-tree ``libvc.so`` built by ``build.py``; there is no
+fallback implementation: if the library is missing, loading raises, and without
+a usable CUDA device every decode / encode returns VC_ERR_IO (4).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvc.so")
+SYNTH_PATH = os.path.join(HERE, "libvcsynth.so")
+
+VC_OK, VC_ERR_FORMAT, VC_ERR_RANGE, VC_ERR_OOM, VC_ERR_IO = 0, 1, 2, 3, 4
+VC_ABSENT, VC_KNOWN_ZERO, VC_PRESENT = 0, 1, 2
+
+# Every symbol the public headers declare (checked by the CPU test suite).
+VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod", "vc_decode_atom",
+              "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
+              "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
+VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
+               "vcg_encode_q",
+               "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
+               "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_last_error", "vcg_profile_enable",
+               "vcg_profile_read", "vcg_last_call_ms"]
+
+
+class Dims(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_uint32), ("ny", ctypes.c_uint32), ("nz", ctypes.c_uint32)]
+
+
+class Box(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in ("x0", "y0", "z0", "x1", "y1", "z1")]
+
+
+P = ctypes.c_void_p
+_lib = None
+_synth = None
+
+
+def build(force=False):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("vc_gb300_build", os.path.join(HERE, "build.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    m.build(force=force)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is not built (run build.py); there is no fallback implementation")
+        L = ctypes.CDLL(LIB_PATH)
+        L.vc_encode.argtypes = [P, Dims, ctypes.c_float, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_size_t)]
+        L.vc_open.restype = P
+        L.vc_open.argtypes = [P, ctypes.c_size_t]
+        L.vc_close.argtypes = [P]
+        L.vc_lod_dims.argtypes = [P, ctypes.c_int, ctypes.POINTER(Dims)]
+        L.vc_decode_lod.argtypes = [P, ctypes.c_int, P, ctypes.POINTER(Dims)]
+        L.vc_decode_atom.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+        L.vc_decode_region.argtypes = [P, ctypes.c_int, Box, P]
+        L.vc_atom_coverage.argtypes = [P, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
+        L.vc_atom_payload_range.argtypes = [P, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                            ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32)]
+        L.vc_archive_version.argtypes = [P]
+        L.vc_region_blob_range.argtypes = [P, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                           ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        L.vc_region_atoms.restype = ctypes.c_uint32
+        L.vcg_decode_region_device.argtypes = [P, ctypes.c_int, Box, P]
+        L.vcg_decode_lod_device.argtypes = [P, ctypes.c_int, P, ctypes.POINTER(Dims)]
+        L.vcg_make_resident.argtypes = [P]
+        L.vcg_encode_device.argtypes = [P, Dims, ctypes.c_float, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_size_t),
+                                        ctypes.POINTER(ctypes.c_float)]
+        L.vcg_encode_q.argtypes = [P, ctypes.c_int, Dims, ctypes.c_float, P, ctypes.POINTER(P),
+                                   ctypes.POINTER(ctypes.c_size_t)]
+        L.vcg_synth_volume_device.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, P]
+        L.vcg_alloc.restype = P
+        L.vcg_alloc.argtypes = [ctypes.c_size_t]
+        L.vcg_free.argtypes = [P]
+        L.vcg_alloc_host.restype = P
+        L.vcg_alloc_host.argtypes = [ctypes.c_size_t]
+        L.vcg_free_host.argtypes = [P]
+        L.vcg_copy.argtypes = [P, P, ctypes.c_size_t]
+        L.vcg_memset.argtypes = [P, ctypes.c_int, ctypes.c_size_t]
+        L.vcg_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+        L.vcg_last_error.restype = ctypes.c_char_p
+        L.vcg_profile_enable.argtypes = [ctypes.c_int]
+        L.vcg_profile_read.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.vcg_last_call_ms.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+_libc = ctypes.CDLL(None)
+_libc.free.argtypes = [P]
+
+
+def ptr(a):
+    return a.ctypes.data_as(P)
+
+
+def last_error():
+    return lib().vcg_last_error().decode()
+
+
+# ---------------------------------------------------------------- device memory
+class DeviceBuffer:
+    """A cudaMalloc'd buffer owned by Python."""
+
+    def __init__(self, nbytes):
+        self.nbytes = int(nbytes)
+        self.ptr = lib().vcg_alloc(self.nbytes)
+        if not self.ptr:
+            raise MemoryError(f"vcg_alloc({nbytes}) failed: {last_error()}")
+
+    def upload(self, arr):
+        a = np.ascontiguousarray(arr)
+        assert a.nbytes <= self.nbytes
+        if lib().vcg_copy(self.ptr, ptr(a), a.nbytes):
+            raise RuntimeError(last_error())
+
+    def download(self, nbytes=None, dtype=np.uint8):
+        n = self.nbytes if nbytes is None else nbytes
+        out = np.empty(n, np.uint8)
+        if lib().vcg_copy(ptr(out), self.ptr, n):
+            raise RuntimeError(last_error())
+        return out.view(dtype)
+
+    def free(self):
+        if self.ptr:
+            lib().vcg_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def sync():
+    return lib().vcg_sync()
+
+
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("ms", ctypes.c_double), ("launches", ctypes.c_uint64),
+                ("bytes_read", ctypes.c_uint64), ("bytes_written", ctypes.c_uint64), ("units", ctypes.c_uint64)]
+
+
+def profile_enable(on=True):
+    lib().vcg_profile_enable(1 if on else 0)
+
+
+def profile_read(reset=True):
+    """Accumulated per-stage kernel statistics {name: {ms, launches, bytes_read, bytes_written, units}}."""
+    arr = (KernelStat * 32)()
+    n = lib().vcg_profile_read(arr, 32, 1 if reset else 0)
+    return {arr[i].name.decode(): {"ms": arr[i].ms, "launches": arr[i].launches, "bytes_read": arr[i].bytes_read,
+                                   "bytes_written": arr[i].bytes_written, "units": arr[i].units}
+            for i in range(min(n, 32))}
+
+
+def last_call_ms():
+    """Device time (CUDA events on the library stream) of this thread's last decode/encode call."""
+    return lib().vcg_last_call_ms()
+
+
+def device_info():
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    s = lib().vcg_device_info(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    return s, a.value, (b.value, c.value)
+
+
+# ---------------------------------------------------------------- codec
+def encode(vol, target_ratio):
+    """vc_encode: (nz, ny, nx) u8 host volume -> (status, archive bytes)."""
+    vol = np.ascontiguousarray(vol, np.uint8)
+    nz, ny, nx = vol.shape
+    out, n = P(), ctypes.c_size_t()
+    s = lib().vc_encode(ptr(vol), Dims(nx, ny, nz), ctypes.c_float(target_ratio), ctypes.byref(out), ctypes.byref(n))
+    if s:
+        return s, None
+    data = ctypes.string_at(out, n.value)
+    _libc.free(out)
+    return s, data
+
+
+def encode_device(dbuf, dims, target_ratio):
+    """vcg_encode_device on a DeviceBuffer holding an (nz, ny, nx) volume."""
+    nx, ny, nz = dims
+    out, n, q0 = P(), ctypes.c_size_t(), ctypes.c_float()
+    s = lib().vcg_encode_device(dbuf.ptr, Dims(nx, ny, nz), ctypes.c_float(target_ratio), ctypes.byref(out),
+                                ctypes.byref(n), ctypes.byref(q0))
+    if s:
+        return s, None, None
+    data = ctypes.string_at(out, n.value)
+    _libc.free(out)
+    return s, data, q0.value
+
+
+def encode_q(vol, target_ratio, qs, on_device=None):
+    """vcg_encode_q: explicit per-LOD base_q. vol: host array or DeviceBuffer (then on_device=dims)."""
+    qa = np.zeros(8, np.float32)
+    qa[:len(qs)] = qs
+    out, n = P(), ctypes.c_size_t()
+    if on_device is None:
+        vol = np.ascontiguousarray(vol, np.uint8)
+        nz, ny, nx = vol.shape
+        s = lib().vcg_encode_q(ptr(vol), 0, Dims(nx, ny, nz), ctypes.c_float(target_ratio), ptr(qa),
+                               ctypes.byref(out), ctypes.byref(n))
+    else:
+        nx, ny, nz = on_device
+        s = lib().vcg_encode_q(vol.ptr, 1, Dims(nx, ny, nz), ctypes.c_float(target_ratio), ptr(qa),
+                               ctypes.byref(out), ctypes.byref(n))
+    if s:
+        return s, None
+    data = ctypes.string_at(out, n.value)
+    _libc.free(out)
+    return s, data
+
+
+class Archive:
+    """An opened archive (vc_open borrows the buffer, so it is kept here)."""
+
+    def __init__(self, data):
+        self.buf = ctypes.create_string_buffer(bytes(data), len(data))
+        self.h = lib().vc_open(ctypes.addressof(self.buf), len(data))
+
+    def __bool__(self):
+        return bool(self.h)
+
+    def close(self):
+        if self.h:
+            lib().vc_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def version(self):
+        return lib().vc_archive_version(self.h)
+
+    def lod_dims(self, lod):
+        d = Dims()
+        s = lib().vc_lod_dims(self.h, lod, ctypes.byref(d))
+        return s, (d.nx, d.ny, d.nz)
+
+    def make_resident(self):
+        return lib().vcg_make_resident(self.h)
+
+    def decode_atom(self, lod, ax, ay, az, out=None):
+        if out is None:
+            out = np.zeros(32768, np.uint8)
+        s = lib().vc_decode_atom(self.h, lod, ax, ay, az, ptr(out))
+        return s, out
+
+    def decode_region(self, lod, box, out=None):
+        x0, y0, z0, x1, y1, z1 = box
+        if out is None:
+            out = np.zeros(max(0, (x1 - x0) * (y1 - y0) * (z1 - z0)), np.uint8)
+        s = lib().vc_decode_region(self.h, lod, Box(*box), ptr(out))
+        return s, out
+
+    def decode_lod(self, lod, out=None):
+        s, (nx, ny, nz) = self.lod_dims(lod)
+        if s:
+            return s, None
+        if out is None:
+            out = np.zeros((nz, ny, nx), np.uint8)
+        d = Dims()
+        s = lib().vc_decode_lod(self.h, lod, ptr(out), ctypes.byref(d))
+        return s, out
+
+    def decode_lod_device(self, lod, dbuf):
+        d = Dims()
+        return lib().vcg_decode_lod_device(self.h, lod, dbuf.ptr, ctypes.byref(d))
+
+    def decode_region_device(self, lod, box, dbuf):
+        return lib().vcg_decode_region_device(self.h, lod, Box(*box), dbuf.ptr)
+
+    def coverage(self, lod, az, ay, ax):
+        return lib().vc_atom_coverage(self.h, lod, az, ay, ax)
+
+    def payload_range(self, lod, az, ay, ax):
+        o, l = ctypes.c_uint64(), ctypes.c_uint32()
+        c = lib().vc_atom_payload_range(self.h, lod, az, ay, ax, ctypes.byref(o), ctypes.byref(l))
+        return c, o.value, l.value
+
+
+# ---------------------------------------------------------------- synthetic volumes
+def synth_lib():
+    global _synth
+    if _synth is None:
+        S = ctypes.CDLL(SYNTH_PATH)
+        S.vcs_cfg_size.restype = ctypes.c_size_t
+        S.vcs_setup.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64]
+        S.vcs_generate.argtypes = [P, P, ctypes.c_int]
+        S.vcs_generate_slab.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, P, ctypes.c_int]
+        _synth = S
+    return _synth
+
+
+def config_seed(config_id):
+    return 0x5EED0000 + config_id
+
+
+def synth(nx, ny, nz, seed, threads=8, z0=0, z1=None):
+    """Host-generated synthetic volume (planes [z0, z1)) as (nz, ny, nx) u8."""
+    S = synth_lib()
+    cfg = ctypes.create_string_buffer(S.vcs_cfg_size())
+    S.vcs_setup(cfg, nx, ny, nz, seed)
+    z1 = nz if z1 is None else z1
+    out = np.zeros((z1 - z0, ny, nx), np.uint8)
+    s = S.vcs_generate_slab(cfg, z0, z1, ptr(out), threads)
+    if s:
+        raise RuntimeError(f"vcs_generate_slab failed ({s})")
+    return out
+
+
+def synth_device(nx, ny, nz, seed):
+    buf = DeviceBuffer(nx * ny * nz + 16)
+    s = lib().vcg_synth_volume_device(nx, ny, nz, seed, buf.ptr)
+    if s:
+        raise RuntimeError(f"vcg_synth_volume_device failed ({s}): {last_error()}")
+    return buf
