@@ -85,24 +85,38 @@ __global__ void __launch_bounds__(1024) k_scan_u64(uint64_t *v, uint64_t n, uint
     if (tid == 0 && total) *total = carry_s;
 }
 
-__global__ void __launch_bounds__(128) k_rc_decode(DecodeJob J) {
-    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= J.n_atoms) return;
-    uint32_t az, ay, ax;
-    box_atom(J, t, az, ay, ax);
-    vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
-    if (e.kind != VCD_PRESENT) { J.cnt[t] = 0; return; }
-    uint32_t cap = 8u * (e.len - 1u) + 64u;
-    if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
-    uint32_t *dst = J.ent + J.ent_off[t];
-    const uint16_t *scan = J.scan;
-    RcDec d;
-    d.init(J.arc + e.off + 1, e.len - 1);
-    uint32_t n = 0;
-    int bad = rc_decode_levels(d, J.band_start, [&](uint32_t p, uint32_t lv) {
-        if (n < cap) dst[n] = (uint32_t)__ldg(scan + p) | (lv << 16);
-        ++n;
-    });
+constexpr int kRcThreads = 128;
+
+__global__ void __launch_bounds__(kRcThreads) k_rc_decode(DecodeJob J) {
+    __shared__ uint32_t bstart[9];
+    if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
+    __syncthreads();
+    // every lane takes part in the warp-lockstep decoder; lanes without a
+    // PRESENT atom run along inactive
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = false;
+    vcd_atom e = {};
+    if (t < J.n_atoms) {
+        uint32_t az, ay, ax;
+        box_atom(J, t, az, ay, ax);
+        e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
+        active = e.kind == VCD_PRESENT;
+        if (!active) J.cnt[t] = 0;
+    }
+    uint32_t cap = 0, n = 0;
+    uint32_t *dst = J.ent;
+    if (active) {
+        cap = 8u * (e.len - 1u) + 64u;
+        if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+        dst = J.ent + J.ent_off[t];
+    }
+    // entries carry the scan position; the transform kernel maps it to raster
+    int bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart,
+                                    [&](uint32_t p, uint32_t lv) {
+                                        if (n < cap) dst[n] = p | (lv << 16);
+                                        ++n;
+                                    });
+    if (!active) return;
     uint32_t flags = (n > cap ? kEntOverflow : 0u) | (bad ? kEntBad : 0u);
     J.cnt[t] = (n > cap ? cap : n) | flags;
     atomicAdd(J.nnz_total, (unsigned long long)(n > cap ? cap : n));
@@ -169,7 +183,7 @@ __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
             const uint32_t *src = J.ent + J.ent_off[t];
             for (uint32_t i = tid; i < n; i += kIdctThreads) {
                 uint32_t w = src[i];
-                T[tile_idx(w & 0xFFFFu)] = (int16_t)(w >> 16);
+                T[tile_idx(__ldg(J.scan + (w & 0xFFFFu)))] = (int16_t)(w >> 16);
             }
         }
         __syncthreads();

@@ -203,27 +203,33 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
 
 template <bool WRITE>
 __global__ void __launch_bounds__(128) k_rc_encode(RcJob J) {
-    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= J.n_atoms) return;
-    const uint32_t meta = J.meta[t];
-    if (meta & kMetaZero) {
-        if (!WRITE) J.len[t] = 0;
-        return;
-    }
+    __shared__ uint32_t bstart[9];
+    if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
+    __syncthreads();
+    // every lane takes part in the warp-lockstep coder; lanes without a
+    // present atom run along inactive
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t meta = t < J.n_atoms ? J.meta[t] : kMetaZero;
+    const bool active = !(meta & kMetaZero);
+    if (!WRITE && t < J.n_atoms && !active) J.len[t] = 0;
     const uint32_t nnz = meta & 0xFFFFu;
-    const uint32_t *ent = J.ent + t * (uint64_t)VCD_MAX_ENTRIES;
+    const uint32_t *ent = J.ent + (active ? t : 0) * (uint64_t)VCD_MAX_ENTRIES;
     if (!WRITE) {
-        uint32_t n = rc_encode_levels<false>(ent, nnz, J.band_start, nullptr);
+        uint32_t n = rc_encode_levels_warp<false>(ent, nnz, active, bstart, nullptr);
+        if (!active) return;
         J.len[t] = n + 1;
         atomicAdd(J.total_bytes, (unsigned long long)(n + 1));
         atomicAdd(J.total_present, 1ull);
         return;
     }
-    const uint64_t a = J.canon_first + t;   // canonical index
-    const uint64_t off = J.pos[a] + (J.lay.first_in_region(a) ? kL2Bytes : 0ull);
-    uint8_t *dst = J.arc + off;
-    dst[0] = (uint8_t)((meta >> 16) & 0xFFu);
-    rc_encode_levels<true>(ent, nnz, J.band_start, dst + 1);
+    uint8_t *dst = nullptr;
+    if (active) {
+        const uint64_t a = J.canon_first + t;   // canonical index
+        const uint64_t off = J.pos[a] + (J.lay.first_in_region(a) ? kL2Bytes : 0ull);
+        dst = J.arc + off;
+        dst[0] = (uint8_t)((meta >> 16) & 0xFFu);
+    }
+    rc_encode_levels_warp<true>(ent, nnz, active, bstart, active ? dst + 1 : nullptr);
 }
 
 // consume[a] = (first atom of its region ? L2 block : 0) + payload length
