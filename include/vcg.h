@@ -35,6 +35,28 @@ vc_status vcg_encode_device(const uint8_t *vol_dev, vc_dims dims, float target_r
 vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
                        const float base_q[VC_NLOD], uint8_t **out_archive, size_t *out_len);
 
+// Decode without allocating (no counterpart in the reference). For callers
+// that cannot let a library allocate device memory: applications that reserve
+// the whole GPU for their own pool up front, so a library cudaMalloc would
+// fail, and latency-bound pipelines that cannot take the device-wide
+// synchronisation that cudaMalloc / cudaFree may cause. Decodes up to
+// VCG_NOALLOC_MAX_ATOMS atom payloads already in device memory: payload i is
+// payload_dev[offsets[i], offsets[i] + lengths[i]) ([dc byte][coder bytes] as
+// stored in an archive, e.g. from vc_atom_payload_range; length 0 = all-zero
+// atom); offsets and lengths are host arrays; base_q is the LOD's base_q. Atom
+// i goes to out_dev + i * VC_ATOM3 (raster z, y, x). payload_dev must be
+// 4-byte aligned and payload_bytes is its size. Returns VC_ERR_RANGE for more
+// than VCG_NOALLOC_MAX_ATOMS atoms, VC_ERR_FORMAT for a range outside the
+// buffer or a malformed payload.
+// Scratch is one fixed device array (about 8 MiB) that every GPU using this
+// library keeps until the process exits; all calls share it and it keeps the
+// last call's contents, so calls whose GPU work overlaps race and must be
+// serialised by the caller. The first call on a device sets the array up
+// (with that device current). Runs on the calling thread's default stream.
+#define VCG_NOALLOC_MAX_ATOMS 64
+vc_status vcg_decode_atoms_noalloc(const uint8_t *payload_dev, size_t payload_bytes, const uint64_t *offsets,
+                                   const uint32_t *lengths, uint32_t n_atoms, float base_q, uint8_t *out_dev);
+
 // Seeded synthetic scroll-sheet volume (the benchmark workload) generated on
 // the device; byte-identical to the host generator in libvcsynth.
 int vcg_synth_volume_device(uint32_t nx, uint32_t ny, uint32_t nz, uint64_t seed, uint8_t *out_dev);

@@ -244,6 +244,19 @@ void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cu
     k_scan_u64<<<1, 1024, 0, s>>>(v, n, base, total);
 }
 
+void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_idct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIdctSmem);
+        attr = true;
+    }
+    if (!J.n_atoms) return;
+    unsigned nb = (unsigned)((J.n_atoms + 127) / 128);
+    k_rc_decode<<<nb, 128, 0, s>>>(J);
+    uint64_t grid = J.n_atoms < (uint64_t)num_sms ? J.n_atoms : (uint64_t)num_sms;
+    k_idct<<<(unsigned)grid, kIdctThreads, kIdctSmem, s>>>(J);
+}
+
 void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev) {
     static bool attr = false;
     if (!attr) {

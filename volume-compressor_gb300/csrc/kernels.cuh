@@ -46,6 +46,9 @@ __host__ __device__ inline void box_atom(const DecodeJob &J, uint64_t t, uint32_
 }
 
 void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev);
+// Range decode + inverse transform only: J.ent_off must already hold each
+// atom's list offset (each list can take VCD_MAX_ENTRIES entries).
+void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s);
 void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cudaStream_t s);
 
 }  // namespace vcg

@@ -22,7 +22,7 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
               "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
                "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_last_error", "vcg_profile_enable",
                "vcg_profile_read", "vcg_last_call_ms"]
@@ -88,6 +88,7 @@ def lib():
         L.vcg_memset.argtypes = [P, ctypes.c_int, ctypes.c_size_t]
         L.vcg_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
         L.vcg_last_error.restype = ctypes.c_char_p
+        L.vcg_decode_atoms_noalloc.argtypes = [P, ctypes.c_size_t, P, P, ctypes.c_uint32, ctypes.c_float, P]
         L.vcg_profile_enable.argtypes = [ctypes.c_int]
         L.vcg_profile_read.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.vcg_last_call_ms.restype = ctypes.c_double
