@@ -71,21 +71,28 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
     __shared__ uint32_t red[32];
     __shared__ uint32_t scanbuf[kFwdThreads / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q.dz[i]; qrr[i] = J.q.rr[i]; }
     for (int i = tid; i < 94 * 32; i += kFwdThreads) rank[i] = J.rank_base[i];
     for (int i = tid; i < 1024; i += kFwdThreads) alt[i] = J.alt_mask[i];
+    int cur_lod = -1;
 
     for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
-        const uint64_t a = J.first_atom + t;   // raster atom index within the LOD
-        const uint32_t ax = (uint32_t)(a % J.acx), ay = (uint32_t)((a / J.acx) % J.acy),
-                       az = (uint32_t)(a / ((uint64_t)J.acx * J.acy));
+        int lod;
+        uint32_t az, ay, ax;
+        J.lay.coords(J.first + t, lod, az, ay, ax);
+        if (lod != cur_lod) {   // uniform across the CTA: quantiser constants of this LOD
+            for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q[lod].dz[i]; qrr[i] = J.q[lod].rr[i]; }
+            cur_lod = lod;
+            __syncthreads();
+        }
+        const uint8_t *vol = J.vol[lod];
+        const uint32_t nx = J.dims[lod][0], ny = J.dims[lod][1], nz = J.dims[lod][2];
         // rows r = tid + 256 j: z = r >> 5, y = r & 31 (lane)
         uint32_t w[4][8];
         uint32_t s = 0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             int r = tid + kFwdThreads * j;
-            load_row(J.vol, J.nx, J.ny, J.nz, ax * 32, ay * 32 + (r & 31), az * 32 + (r >> 5), w[j]);
+            load_row(vol, nx, ny, nz, ax * 32, ay * 32 + (r & 31), az * 32 + (r >> 5), w[j]);
 #pragma unroll
             for (int i = 0; i < 8; ++i) s = __dp4a(w[j][i], 0x01010101u, s);
         }

@@ -36,13 +36,15 @@ struct Layout {
     }
 };
 
+// Forward pass over canonical atoms [first, first + n_atoms) of the pyramid
+// (any mix of LODs).
 struct FwdJob {
-    const uint8_t *vol;          // LOD volume (x fastest)
-    uint32_t nx, ny, nz;
-    uint32_t acx, acy;
-    uint64_t first_atom;         // raster index within the LOD of this chunk's first atom
+    Layout lay;
+    const uint8_t *vol[8];       // LOD volumes (x fastest)
+    uint32_t dims[8][3];         // nx, ny, nz per LOD
+    uint64_t first;              // canonical index of this launch's first atom
     uint64_t n_atoms;
-    vcd_quant q;                 // per-class quantiser constants
+    const vcd_quant *q;          // per-LOD quantiser constants (device, [lod])
     const uint16_t *rank_base;
     const uint32_t *alt_mask;
     uint32_t *ent;               // per atom VCD_MAX_ENTRIES slots: scan position | level << 16

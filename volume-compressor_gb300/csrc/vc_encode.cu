@@ -14,7 +14,7 @@
 
 using namespace vcg;
 
-static const uint64_t kChunk = 8192;   // atoms per forward/coder batch (1 GiB of list scratch)
+static const uint64_t kChunk = 32768;   // atoms per forward/coder launch (4 GiB of list scratch)
 
 static inline float f_of(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
 static inline uint32_t b_of(float f) { uint32_t b; memcpy(&b, &f, 4); return b; }
@@ -37,23 +37,30 @@ struct EncState {
     uint64_t *pos;
     uint8_t *dc, *arc;
     unsigned long long *red;
+    vcd_quant *qtab;          // device, per LOD
+    vcd_quant qh;             // host staging
 };
 
-// Forward + coder pass over LOD `lod` at `q`: size-only (lengths into len and
-// the totals) or writing payloads into the archive.
-static int run_lod(EncState &S, int lod, float q, bool write) {
-    vcd_quant qc;
-    vch_quant_consts(q, &qc);
-    const uint64_t na = S.lay.base[lod + 1] - S.lay.base[lod];
-    for (uint64_t a0 = 0; a0 < na; a0 += kChunk) {
-        const uint64_t n = na - a0 < kChunk ? na - a0 : kChunk;
+// Quantiser constants of `lod` at q, into the device table.
+static void set_q(EncState &S, int lod, float q) {
+    vch_quant_consts(q, &S.qh);
+    cudaMemcpyAsync(S.qtab + lod, &S.qh, sizeof(vcd_quant), cudaMemcpyHostToDevice, S.c->stream);
+}
+
+// Forward + coder passes over canonical atoms [a0, a1) (any mix of LODs, each at
+// the q in the device table): size-only (lengths into len and the totals) or
+// writing payloads into the archive. One launch pair per kChunk atoms: a coder
+// launch costs about one atom's serial coding time however many atoms it holds.
+static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
+    for (uint64_t c0 = a0; c0 < a1; c0 += kChunk) {
+        const uint64_t n = a1 - c0 < kChunk ? a1 - c0 : kChunk;
         FwdJob F;
-        F.vol = S.lvol[lod];
-        F.nx = S.dims[lod][0]; F.ny = S.dims[lod][1]; F.nz = S.dims[lod][2];
-        F.acx = S.lay.acx[lod]; F.acy = S.lay.acy[lod];
-        F.first_atom = a0;
+        F.lay = S.lay;
+        memcpy(F.vol, S.lvol, sizeof F.vol);
+        memcpy(F.dims, S.dims, sizeof F.dims);
+        F.first = c0;
         F.n_atoms = n;
-        F.q = qc;
+        F.q = S.qtab;
         F.rank_base = g_dev.tables->rank_base;
         F.alt_mask = g_dev.tables->alt_mask;
         F.ent = S.ent;
@@ -68,22 +75,22 @@ static int run_lod(EncState &S, int lod, float q, bool write) {
         R.ent = S.ent;
         memcpy(R.band_start, g_dev.band_start, sizeof R.band_start);
         if (!write) {
-            R.len = S.len + S.lay.base[lod] + a0;
+            R.len = S.len + c0;
             R.total_bytes = S.red;
             R.total_present = S.red + 1;
         } else {
             R.arc = S.arc;
             R.pos = S.pos;
-            R.canon_first = S.lay.base[lod] + a0;
+            R.canon_first = c0;
             R.lay = S.lay;
-            launch_gather_dc(S.meta, n, S.dc + S.lay.base[lod] + a0, S.c->stream);
+            launch_gather_dc(S.meta, n, S.dc + c0, S.c->stream);
         }
         if (prof) cudaEventRecord(S.c->ev[5], S.c->stream);
         launch_rc_encode(R, write, S.c->stream);
         if (prof) {
             cudaEventRecord(S.c->ev[1], S.c->stream);
             cudaEventSynchronize(S.c->ev[1]);
-            // forward: volume bytes of the chunk in, coefficient lists out (not counted: scratch)
+            // forward: volume bytes in (the lists it writes are scratch, not counted)
             vcd_prof_add("fwd_dct_quant", vcd_elapsed(S.c->ev[4], S.c->ev[5]), 1, n * 32768ull, 0, n);
             vcd_prof_add(write ? "rc_encode_write" : "rc_encode_size", vcd_elapsed(S.c->ev[5], S.c->ev[1]), 1, 0,
                          0, n);
@@ -134,14 +141,17 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
             q += nvox[l];
         }
     }
-    CK(vcd_scratch(c, VCD_BUF_EENT, kChunk * VCD_MAX_ENTRIES * 4, &p), "coefficient lists");
+    const uint64_t chunk = total_atoms < kChunk ? total_atoms : kChunk;
+    CK(vcd_scratch(c, VCD_BUF_EENT, chunk * VCD_MAX_ENTRIES * 4 + 16, &p), "coefficient lists");
     S.ent = (uint32_t *)p;
     const uint64_t na0 = S.lay.base[1];
-    // meta (chunk) | len (all atoms) | best LOD0 len | dc (all atoms)
-    size_t meta_b = kChunk * 4, len_b = total_atoms * 4, best_b = na0 * 4, dc_b = total_atoms + 16;
-    CK(vcd_scratch(c, VCD_BUF_EMETA, meta_b + len_b + best_b + dc_b + 64, &p), "encode metadata");
-    S.meta = (uint32_t *)p;
-    S.len = S.meta + kChunk;
+    // quant table (8 LODs) | meta (chunk) | len (all atoms) | best LOD0 len | dc (all atoms)
+    size_t q_b = 8 * sizeof(vcd_quant), meta_b = chunk * 4, len_b = total_atoms * 4, best_b = na0 * 4;
+    size_t dc_b = total_atoms + 16;
+    CK(vcd_scratch(c, VCD_BUF_EMETA, q_b + meta_b + len_b + best_b + dc_b + 64, &p), "encode metadata");
+    S.qtab = (vcd_quant *)p;
+    S.meta = (uint32_t *)((uint8_t *)p + q_b);
+    S.len = S.meta + chunk;
     S.best = S.len + total_atoms;
     S.dc = (uint8_t *)(S.best + na0);
     CK(vcd_scratch(c, VCD_BUF_POS, (total_atoms + 1) * 8, &p), "placement");
@@ -159,7 +169,8 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
         uint32_t mid = lo + (hi - lo) / 2;
         float q = f_of(mid);
         CK(cudaMemsetAsync(S.red, 0, 16, st), "totals reset");
-        run_lod(S, 0, q, false);
+        set_q(S, 0, q);
+        run_range(S, 0, na0, false);
         unsigned long long h[2];
         CK(cudaMemcpyAsync(h, S.red, 16, cudaMemcpyDeviceToHost, st), "totals read");
         CK(cudaStreamSynchronize(st), "rate control pass");
@@ -188,13 +199,14 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
         for (int l = 0; l < nlod; ++l) { qs[l] = vch_clamp_q(q < 0.05f ? 0.05f : q); q = q * 0.6f; }
     }
 
-    // ---- sizes of every atom at its LOD's q
+    // ---- sizes of every atom at its LOD's q (LODs 1.. together in one pass)
+    for (int l = 0; l < nlod; ++l) set_q(S, l, qs[l]);
     if (have_best) CK(cudaMemcpyAsync(S.len, S.best, na0 * 4, cudaMemcpyDeviceToDevice, st), "restore sizes");
     else {
         CK(cudaMemsetAsync(S.red, 0, 16, st), "totals reset");
-        run_lod(S, 0, qs[0], false);
+        run_range(S, 0, na0, false);
     }
-    for (int l = 1; l < nlod; ++l) run_lod(S, l, qs[l], false);
+    run_range(S, na0, total_atoms, false);
 
     // ---- canonical placement: exclusive scan of consumed bytes
     const uint64_t head = 128 + 16 * info->l1_cap;
@@ -219,7 +231,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     S.arc = (uint8_t *)p;
     P.arc = S.arc;
     cudaMemsetAsync(S.arc, 0, total, st);
-    for (int l = 0; l < nlod; ++l) run_lod(S, l, qs[l], true);
+    run_range(S, 0, total_atoms, true);
     launch_slots(P, st);
     cudaEventRecord(c->ev[7], st);   // device work ends (the archive head and copy-out follow)
 
