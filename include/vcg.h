@@ -19,6 +19,25 @@ extern "C" {
 vc_status vcg_decode_region_device(vc_archive *a, int lod, vc_box box, uint8_t *out_dev);
 vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev, vc_dims *out_dims);
 
+// Batched region decode: many boxes (any LODs, sizes and offsets) of one
+// archive in one device pass. Every distinct atom the batch touches is decoded
+// once and cropped into each box that overlaps it. status[i] is what
+// vc_decode_region would return for request i, and outputs follow its rules
+// (a request that meets a bad atom gets only the atoms before it, z-y-x order).
+// out_on_device != 0: every out is device memory; else host memory. The launch
+// shape is autotuned on the calling thread's first batch; later batches replay
+// one CUDA graph.
+typedef struct {
+    int32_t lod;
+    vc_box box;
+    uint8_t *out;   // (x1-x0)*(y1-y0)*(z1-z0) bytes, raster (z, y, x)
+} vcg_region_request;
+vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_request *reqs, int out_on_device,
+                             vc_status *status);
+// Launch shape chosen by the autotuner for the calling thread (0 before the
+// first batch): range-decoder CTA size and transform CTA size (32 x warps per atom).
+void vcg_batch_shape(int *rc_threads, int *transform_threads);
+
 // Resolve the archive's atom table and copy archive + table into device
 // memory now (otherwise done on the first decode).
 vc_status vcg_make_resident(vc_archive *a);

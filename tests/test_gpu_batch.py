@@ -1,0 +1,75 @@
+"""Batched region decode (vcg_decode_regions): every request equals the plain
+vc_decode_region result (status and bytes), for host and device outputs,
+across graph replays, buffer growth and a corrupt archive."""
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import load_archive
+
+pytestmark = pytest.mark.gpu
+
+
+def random_requests(a, rng, n, max_lod, max_edge=90, invalid=0):
+    reqs = []
+    for _ in range(n):
+        lod = int(rng.integers(0, max_lod + 1))
+        _, d = a.lod_dims(lod)
+        e = [int(rng.integers(1, min(max_edge, d[k]) + 1)) for k in range(3)]
+        o = [int(rng.integers(0, d[k] - e[k] + 1)) for k in range(3)]
+        reqs.append((lod, (o[0], o[1], o[2], o[0] + e[0], o[1] + e[1], o[2] + e[2])))
+    for _ in range(invalid):
+        reqs.insert(int(rng.integers(0, len(reqs) + 1)), (0, (5, 5, 5, 5, 9, 9)))   # empty box -> RANGE
+    return reqs
+
+
+def box_bytes(box):
+    x0, y0, z0, x1, y1, z1 = box
+    return max(0, (x1 - x0) * (y1 - y0) * (z1 - z0))
+
+
+def check(vc, a, reqs, on_device):
+    if on_device:
+        outs = [vc.DeviceBuffer(max(1, box_bytes(b))) for _, b in reqs]
+    else:
+        outs = [np.full(max(1, box_bytes(b)), 0x5A, np.uint8) for _, b in reqs]
+    s, st = a.decode_regions(reqs, outs, on_device)
+    assert s == vc.VC_OK
+    for i, (lod, box) in enumerate(reqs):
+        ref = np.full(max(1, box_bytes(box)), 0x5A, np.uint8)
+        s2, _ = a.decode_region(lod, box, ref)
+        assert st[i] == s2, (i, lod, box)
+        got = outs[i].download(max(1, box_bytes(box))) if on_device else outs[i]
+        if s2 == vc.VC_OK:
+            assert np.array_equal(got, ref), (i, lod, box)
+
+
+@pytest.mark.parametrize("name", ["synth_prime_97x131x65_t20", "ref_test_basic", "synth_64_t10"])
+def test_batch_matches_plain_host_and_device(vc, gpu, golden, name):
+    a = vc.Archive(load_archive(golden[name]))
+    rng = np.random.default_rng(11)
+    nlod = struct.unpack_from("<I", load_archive(golden[name]), 20)[0]
+    check(vc, a, random_requests(a, rng, 60, min(nlod - 1, 3), invalid=3), on_device=False)
+    check(vc, a, random_requests(a, rng, 60, min(nlod - 1, 3), invalid=2), on_device=True)
+    rc, tx = vc.batch_shape()
+    assert rc in (64, 128, 256) and tx in (256, 512)
+
+
+def test_batch_graph_replay_and_growth(vc, gpu, golden):
+    a = vc.Archive(load_archive(golden["synth_prime_97x131x65_t20"]))
+    rng = np.random.default_rng(12)
+    for n, edge in [(10, 40), (10, 40), (200, 97), (5, 20), (300, 130)]:   # replays, then larger buffers
+        check(vc, a, random_requests(a, rng, n, 2, max_edge=edge), on_device=True)
+
+
+def test_batch_on_corrupt_archive_matches_plain(vc, gpu, golden):
+    from test_gpu_decode import _slot_offset
+    data = bytearray(load_archive(golden["synth_prime_97x131x65_t20"]))
+    so = _slot_offset(data, 0, 1, 2, 1)   # break the payload range of LOD0 atom (1, 2, 1)
+    struct.pack_into("<I", data, so + 8, len(data))
+    a = vc.Archive(bytes(data))
+    rng = np.random.default_rng(13)
+    reqs = random_requests(a, rng, 40, 1, max_edge=97) + [(0, (0, 0, 0, 97, 131, 65))]
+    check(vc, a, reqs, on_device=False)
+    check(vc, a, reqs, on_device=True)

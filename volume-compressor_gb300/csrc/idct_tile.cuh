@@ -1,0 +1,126 @@
+// Shared pieces of the inverse-transform kernels (device): level scatter into a
+// swizzled shared-memory tile, dequantisation, inverse passes along x and y per
+// slab, the pass along z per column, and the cropped store into a box raster.
+#pragma once
+#include <stdint.h>
+
+#include "dct32.cuh"
+#include "kernels.cuh"
+#include "rangecoder.cuh"
+
+namespace vcg {
+
+__device__ __forceinline__ int tile_idx(uint32_t r) {   // raster (kz,ky,kx) -> swizzled slab slot
+    return (int)((r >> 10) << 10) | swz((int)((r >> 5) & 31u), (int)(r & 31u));
+}
+
+// dequantised coefficient of raw level l at raster r (src/vc/vc.c:327-338, i32 wrap)
+__device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t *dqs, const int32_t *dqb,
+                                           const uint32_t *alt) {
+    uint32_t f = (r >> 10) + ((r >> 5) & 31u) + (r & 31u);
+    uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
+    uint32_t m = (uint32_t)(l < 0 ? -l : l);
+    int32_t v = (int32_t)(m * (uint32_t)dqs[cls] + (uint32_t)dqb[cls] + 128u) >> 8;
+    return l == 0 ? 0 : (l < 0 ? (int32_t)(0u - (uint32_t)v) : v);
+}
+
+// Tile of one PRESENT atom after the inverse passes along x and y: levels
+// scattered into T (32 slabs x swizzled 32x32, i32), dequantised while each
+// slab is loaded, then one warp per slab (lane per line). Ends with a barrier.
+template <int NT>
+__device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, const vcd_atom &e, uint32_t c,
+                                             const uint32_t *src, const uint16_t *scan, const uint32_t *band_start,
+                                             const int32_t *dqs, const int32_t *dqb, const uint32_t *alt) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int4 *T4 = reinterpret_cast<int4 *>(T);
+    for (int i = tid; i < 32768 / 4; i += NT) T4[i] = make_int4(0, 0, 0, 0);
+    __syncthreads();
+    if (c & kEntOverflow) {
+        // slow path for streams whose list exceeded its capacity
+        if (tid == 0) {
+            RcDec d;
+            d.init(arc + e.off + 1, e.len - 1);
+            rc_decode_levels(d, band_start, [&](uint32_t p, uint32_t lv) { T[tile_idx(scan[p])] = (int16_t)lv; });
+        }
+    } else {
+        const uint32_t n = c & kEntMask;
+        for (uint32_t i = tid; i < n; i += NT) {
+            uint32_t w = src[i];
+            T[tile_idx(__ldg(scan + (w & 0xFFFFu)))] = (int16_t)(w >> 16);
+        }
+    }
+    __syncthreads();
+    for (int kz = warp; kz < 32; kz += NT / 32) {
+        int32_t *S = T + kz * 1024;
+        int32_t v[32], o[32];
+        int any = 0;
+#pragma unroll
+        for (int kx = 0; kx < 32; ++kx) {
+            int32_t l = S[swz(lane, kx)];
+            v[kx] = dequant(l, (uint32_t)(kz * 1024 + lane * 32 + kx), dqs, dqb, alt);
+            any |= v[kx];
+        }
+        if (__any_sync(0xFFFFFFFFu, any)) {
+            idct32_line(v, o);
+#pragma unroll
+            for (int x = 0; x < 32; ++x) S[swz(lane, x)] = o[x];
+            __syncwarp();
+#pragma unroll
+            for (int ky = 0; ky < 32; ++ky) v[ky] = S[swz(ky, lane)];
+            idct32_line(v, o);
+            __syncwarp();
+#pragma unroll
+            for (int y = 0; y < 32; ++y) S[swz(y, lane)] = o[y];
+        } else {
+#pragma unroll
+            for (int x = 0; x < 32; ++x) S[swz(lane, x)] = 0;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+}
+
+// Pass along z for column (y, x = lane): voxel values before +dc.
+__device__ __forceinline__ void idct_col_z(const int32_t *T, int y, int lane, int32_t (&o)[32]) {
+    int32_t v[32];
+#pragma unroll
+    for (int kz = 0; kz < 32; ++kz) v[kz] = T[kz * 1024 + swz(y, lane)];
+    idct32_line(v, o);
+}
+
+// Crop window of atom origin g (voxels) inside box [b0, b1) on one axis, atom-local.
+struct Crop {
+    uint32_t lx0, lx1, ly0, ly1, lz0, lz1;
+    __device__ __forceinline__ void set(uint32_t gx, uint32_t gy, uint32_t gz, uint32_t x0, uint32_t y0, uint32_t z0,
+                                        uint32_t x1, uint32_t y1, uint32_t z1) {
+        lx0 = x0 > gx ? x0 - gx : 0; lx1 = x1 < gx + 32 ? x1 - gx : 32;
+        ly0 = y0 > gy ? y0 - gy : 0; ly1 = y1 < gy + 32 ? y1 - gy : 32;
+        lz0 = z0 > gz ? z0 - gz : 0; lz1 = z1 < gz + 32 ? z1 - gz : 32;
+    }
+};
+
+// Store column (y, lane) of the atom (o + dc, clamped) into the crop window;
+// obase points at the window's first voxel inside a box raster of pitch ox, oy.
+__device__ __forceinline__ void store_col(uint8_t *obase, uint64_t ox, uint64_t oy, const Crop &k, int y, int lane,
+                                          const int32_t (&o)[32], int32_t dc) {
+    if ((uint32_t)lane < k.lx0 || (uint32_t)lane >= k.lx1 || (uint32_t)y < k.ly0 || (uint32_t)y >= k.ly1) return;
+    uint8_t *col = obase + (uint64_t)(y - k.ly0) * ox + (lane - k.lx0);
+#pragma unroll
+    for (int z = 0; z < 32; ++z) {
+        if ((uint32_t)z >= k.lz0 && (uint32_t)z < k.lz1) {
+            int32_t x = (int32_t)((uint32_t)o[z] + (uint32_t)dc);
+            col[(uint64_t)(z - k.lz0) * oy * ox] = (uint8_t)(x < 0 ? 0 : x > 255 ? 255 : x);
+        }
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void zero_window(uint8_t *obase, uint64_t ox, uint64_t oy, const Crop &k) {
+    const uint32_t cw = k.lx1 - k.lx0, ch = k.ly1 - k.ly0, cd = k.lz1 - k.lz0;
+    for (uint32_t i = threadIdx.x; i < cw * ch * cd; i += NT) {
+        uint32_t x = i % cw, y = (i / cw) % ch, z = i / (cw * ch);
+        obase[((uint64_t)z * oy + y) * ox + x] = 0;
+    }
+}
+
+}  // namespace vcg

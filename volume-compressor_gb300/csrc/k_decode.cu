@@ -16,6 +16,7 @@
 
 #include "dct32.cuh"
 #include "kernels.cuh"
+#include "idct_tile.cuh"
 #include "rangecoder.cuh"
 
 namespace vcg {
@@ -123,20 +124,6 @@ __global__ void __launch_bounds__(kRcThreads) k_rc_decode(DecodeJob J) {
     if (bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
 }
 
-__device__ __forceinline__ int tile_idx(uint32_t r) {   // raster (kz,ky,kx) -> swizzled slab slot
-    return (int)((r >> 10) << 10) | swz((int)((r >> 5) & 31u), (int)(r & 31u));
-}
-
-// dequantised coefficient of raw level l at raster r (src/vc/vc.c:327-338, i32 wrap)
-__device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t *dqs, const int32_t *dqb,
-                                           const uint32_t *alt) {
-    uint32_t f = (r >> 10) + ((r >> 5) & 31u) + (r & 31u);
-    uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
-    uint32_t m = (uint32_t)(l < 0 ? -l : l);
-    int32_t v = (int32_t)(m * (uint32_t)dqs[cls] + (uint32_t)dqb[cls] + 128u) >> 8;
-    return l == 0 ? 0 : (l < 0 ? (int32_t)(0u - (uint32_t)v) : v);
-}
-
 __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
     extern __shared__ int32_t T[];   // 32 slabs x swizzled 32x32
     __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
@@ -150,91 +137,21 @@ __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
         uint32_t az, ay, ax;
         box_atom(J, t, az, ay, ax);
         const vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
-        // crop window of this atom inside the box, atom-local coordinates
+        Crop k;
         const uint32_t gx = ax * 32, gy = ay * 32, gz = az * 32;
-        const uint32_t lx0 = J.x0 > gx ? J.x0 - gx : 0, lx1 = J.x1 < gx + 32 ? J.x1 - gx : 32;
-        const uint32_t ly0 = J.y0 > gy ? J.y0 - gy : 0, ly1 = J.y1 < gy + 32 ? J.y1 - gy : 32;
-        const uint32_t lz0 = J.z0 > gz ? J.z0 - gz : 0, lz1 = J.z1 < gz + 32 ? J.z1 - gz : 32;
-        uint8_t *obase = J.out + ((uint64_t)(gz + lz0 - J.z0) * J.oy + (gy + ly0 - J.y0)) * J.ox + (gx + lx0 - J.x0);
-        const uint32_t cw = lx1 - lx0, ch = ly1 - ly0, cd = lz1 - lz0;
+        k.set(gx, gy, gz, J.x0, J.y0, J.z0, J.x1, J.y1, J.z1);
+        uint8_t *obase = J.out + ((uint64_t)(gz + k.lz0 - J.z0) * J.oy + (gy + k.ly0 - J.y0)) * J.ox + (gx + k.lx0 - J.x0);
         const uint32_t c = e.kind == VCD_PRESENT ? J.cnt[t] : kEntBad;
         if (e.kind != VCD_PRESENT || (c & kEntBad)) {   // ABSENT / KNOWN_ZERO -> zeros
-            for (uint32_t i = tid; i < cw * ch * cd; i += kIdctThreads) {
-                uint32_t x = i % cw, y = (i / cw) % ch, z = i / (cw * ch);
-                obase[((uint64_t)z * J.oy + y) * J.ox + x] = 0;
-            }
+            zero_window<kIdctThreads>(obase, J.ox, J.oy, k);
             continue;
         }
         const int32_t dc = J.arc[e.off];
-        int4 *T4 = reinterpret_cast<int4 *>(T);
-        for (int i = tid; i < 32768 / 4; i += kIdctThreads) T4[i] = make_int4(0, 0, 0, 0);
-        __syncthreads();
-        if (c & kEntOverflow) {
-            // slow path for streams whose list exceeded its capacity
-            if (tid == 0) {
-                RcDec d;
-                d.init(J.arc + e.off + 1, e.len - 1);
-                rc_decode_levels(d, J.band_start, [&](uint32_t p, uint32_t lv) {
-                    T[tile_idx(J.scan[p])] = (int16_t)lv;
-                });
-            }
-        } else {
-            const uint32_t n = c & kEntMask;
-            const uint32_t *src = J.ent + J.ent_off[t];
-            for (uint32_t i = tid; i < n; i += kIdctThreads) {
-                uint32_t w = src[i];
-                T[tile_idx(__ldg(J.scan + (w & 0xFFFFu)))] = (int16_t)(w >> 16);
-            }
-        }
-        __syncthreads();
-
-        // passes along x then y, one warp per z-slab
-        for (int kz = warp; kz < 32; kz += kIdctThreads / 32) {
-            int32_t *S = T + kz * 1024;
-            int32_t v[32], o[32];
-            int any = 0;
-#pragma unroll
-            for (int kx = 0; kx < 32; ++kx) {
-                int32_t l = S[swz(lane, kx)];
-                v[kx] = dequant(l, (uint32_t)(kz * 1024 + lane * 32 + kx), dqs, dqb, alt);
-                any |= v[kx];
-            }
-            if (__any_sync(0xFFFFFFFFu, any)) {
-                idct32_line(v, o);
-#pragma unroll
-                for (int x = 0; x < 32; ++x) S[swz(lane, x)] = o[x];
-                __syncwarp();
-#pragma unroll
-                for (int ky = 0; ky < 32; ++ky) v[ky] = S[swz(ky, lane)];
-                idct32_line(v, o);
-                __syncwarp();
-#pragma unroll
-                for (int y = 0; y < 32; ++y) S[swz(y, lane)] = o[y];
-            } else {
-#pragma unroll
-                for (int x = 0; x < 32; ++x) S[swz(lane, x)] = 0;
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-
-        // pass along z: thread = column (y, x = lane); store the cropped voxels
+        idct_tile_xy<kIdctThreads>(T, J.arc, e, c, J.ent + J.ent_off[t], J.scan, J.band_start, dqs, dqb, alt);
         for (int y = warp; y < 32; y += kIdctThreads / 32) {
-            int32_t v[32], o[32];
-#pragma unroll
-            for (int kz = 0; kz < 32; ++kz) v[kz] = T[kz * 1024 + swz(y, lane)];
-            idct32_line(v, o);
-            const bool in_xy = (uint32_t)lane >= lx0 && (uint32_t)lane < lx1 && (uint32_t)y >= ly0 && (uint32_t)y < ly1;
-            if (in_xy) {
-                uint8_t *col = obase + (uint64_t)(y - ly0) * J.ox + (lane - lx0);
-#pragma unroll
-                for (int z = 0; z < 32; ++z) {
-                    if ((uint32_t)z >= lz0 && (uint32_t)z < lz1) {
-                        int32_t x = (int32_t)((uint32_t)o[z] + (uint32_t)dc);
-                        col[(uint64_t)(z - lz0) * J.oy * J.ox] = (uint8_t)(x < 0 ? 0 : x > 255 ? 255 : x);
-                    }
-                }
-            }
+            int32_t o[32];
+            idct_col_z(T, y, lane, o);
+            store_col(obase, J.ox, J.oy, k, y, lane, o, dc);
         }
         __syncthreads();
     }

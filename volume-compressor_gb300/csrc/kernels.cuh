@@ -45,6 +45,33 @@ __host__ __device__ inline void box_atom(const DecodeJob &J, uint64_t t, uint32_
     az = J.baz + (uint32_t)(t / ((uint64_t)J.bnx * J.bny));
 }
 
+// ---- batched region decode: every distinct atom of a batch of boxes is decoded
+// once and cropped into each box that overlaps it.
+using BoxReq = vcd_boxreq;
+using UAtom = vcd_uatom;
+struct BatchJob {
+    const uint8_t *arc;
+    const vcd_atom *atoms;       // archive atom table (all LODs)
+    const UAtom *ua;
+    const uint32_t *dst;         // request ids, grouped per distinct atom
+    const BoxReq *reqs;
+    const uint32_t *n_ua;        // device: number of distinct atoms (read at run time)
+    uint32_t *ent;
+    const uint64_t *ent_off;     // per distinct atom
+    uint32_t *cnt;
+    const vcd_dq *dq;            // per LOD
+    const uint32_t *alt_mask;
+    const uint16_t *scan;
+    uint32_t *work;              // transform work counter (reset per batch)
+    uint32_t *req_err;           // per request: set when one of its atoms is malformed
+    uint32_t band_start[9];
+};
+struct BatchShape {              // tunables the autotuner chooses among
+    int rc_threads;              // range-decoder CTA size: 64, 128, 256
+    int idct_threads;            // transform CTA size (warps per atom x 32): 256 or 512
+};
+void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s);
+
 void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev);
 // Range decode + inverse transform only: J.ent_off must already hold each
 // atom's list offset (each list can take VCD_MAX_ENTRIES entries).

@@ -1,0 +1,160 @@
+// Batched region decode orchestration: upload the batch description (distinct
+// atoms, their destination lists, the request boxes, list offsets) into
+// grow-only device buffers, then replay one CUDA graph of the persistent
+// range-decode + transform launches. The launch shape (range-decoder CTA size,
+// transform CTA size) is picked once per host thread by timing every candidate
+// on the first batch (all candidates produce identical bytes).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "kernels.cuh"
+#include "vc_device.h"
+
+using namespace vcg;
+
+#define VC_API extern "C" __attribute__((visibility("default")))
+
+static const BatchShape kShapes[] = {{64, 256}, {128, 256}, {256, 256}, {64, 512}, {128, 512}, {256, 512}};
+
+#define CKB(call, what)                                \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) {                       \
+            vcd_set_error(what, e_);                   \
+            return vcd_status_of(e_);                  \
+        }                                              \
+    } while (0)
+
+static size_t cap_of(const vcd_ctx *c, int slot) { return c->cap[slot]; }
+
+extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *const *host_out, uint32_t *req_err) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    cudaStream_t st = c->stream;
+    if (b->n_req == 0) return 0;
+    void *p_ua, *p_dst, *p_req, *p_off, *p_cnt, *p_ent, *p_ctl, *p_out = NULL;
+    CKB(vcd_scratch(c, VCD_BUF_BUA, (size_t)b->n_ua * sizeof(vcd_uatom) + 64, &p_ua), "batch atoms");
+    CKB(vcd_scratch(c, VCD_BUF_BDST, (size_t)b->n_dst * 4 + 64, &p_dst), "batch destinations");
+    CKB(vcd_scratch(c, VCD_BUF_BREQ, (size_t)b->n_req * sizeof(vcd_boxreq) + 64, &p_req), "batch requests");
+    CKB(vcd_scratch(c, VCD_BUF_BOFF, (size_t)b->n_ua * 8 + 64, &p_off), "batch list offsets");
+    CKB(vcd_scratch(c, VCD_BUF_BCNT, (size_t)b->n_ua * 4 + 64, &p_cnt), "batch counts");
+    CKB(vcd_scratch(c, VCD_BUF_BENT, b->cap_total * 4 + 64, &p_ent), "batch lists");
+    CKB(vcd_scratch(c, VCD_BUF_BCTL, 16 + (size_t)b->n_req * 4 + 64, &p_ctl), "batch control");
+    uint64_t out_total = 0;
+    if (host_out) {   // outputs staged in one device arena
+        for (uint32_t i = 0; i < b->n_req; ++i) {
+            const vcd_boxreq &r = b->reqs[i];
+            out_total += ((uint64_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0) + 15) & ~15ull;
+        }
+        CKB(vcd_scratch(c, VCD_BUF_BOUT, out_total + 16, &p_out), "batch outputs");
+        uint64_t o = 0;
+        for (uint32_t i = 0; i < b->n_req; ++i) {
+            vcd_boxreq &r = b->reqs[i];
+            r.out = (uint8_t *)p_out + o;
+            o += ((uint64_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0) + 15) & ~15ull;
+        }
+    }
+    uint32_t *ctl = (uint32_t *)p_ctl;   // [0] distinct atoms, [1] work counter, [4..] per-request errors
+    CKB(cudaMemcpyAsync(p_ua, b->ua, (size_t)b->n_ua * sizeof(vcd_uatom), cudaMemcpyHostToDevice, st), "upload");
+    CKB(cudaMemcpyAsync(p_dst, b->dst, (size_t)b->n_dst * 4, cudaMemcpyHostToDevice, st), "upload");
+    CKB(cudaMemcpyAsync(p_req, b->reqs, (size_t)b->n_req * sizeof(vcd_boxreq), cudaMemcpyHostToDevice, st), "upload");
+    CKB(cudaMemcpyAsync(p_off, b->ent_off, (size_t)b->n_ua * 8, cudaMemcpyHostToDevice, st), "upload");
+    CKB(cudaMemsetAsync(p_ctl, 0, 16 + (size_t)b->n_req * 4, st), "reset");
+    CKB(cudaMemcpyAsync(ctl, &b->n_ua, 4, cudaMemcpyHostToDevice, st), "upload");
+
+    BatchJob J;
+    memset(&J, 0, sizeof J);
+    J.arc = d->arc;
+    J.atoms = d->atoms;
+    J.ua = (const UAtom *)p_ua;
+    J.dst = (const uint32_t *)p_dst;
+    J.reqs = (const BoxReq *)p_req;
+    J.n_ua = ctl;
+    J.ent = (uint32_t *)p_ent;
+    J.ent_off = (const uint64_t *)p_off;
+    J.cnt = (uint32_t *)p_cnt;
+    J.dq = d->dq;
+    J.alt_mask = g_dev.tables->alt_mask;
+    J.scan = g_dev.tables->scan;
+    J.work = ctl + 1;
+    J.req_err = ctl + 4;
+    memcpy(J.band_start, g_dev.band_start, sizeof J.band_start);
+    // capacity in distinct atoms the range-decode grid must cover (the buffer's)
+    const uint32_t max_ua = (uint32_t)((cap_of(c, VCD_BUF_BUA) - 64) / sizeof(vcd_uatom));
+
+    if (!c->batch_rc_threads) {   // autotune on this first batch
+        float best = 1e30f;
+        for (const BatchShape &s : kShapes) {
+            CKB(cudaMemsetAsync(ctl + 1, 0, 4, st), "reset");
+            cudaEventRecord(c->ev[0], st);
+            launch_batch(J, s, g_dev.num_sms, max_ua, st);
+            cudaEventRecord(c->ev[1], st);
+            CKB(cudaEventSynchronize(c->ev[1]), "autotune");
+            CKB(cudaGetLastError(), "autotune");
+            float ms = vcd_elapsed(c->ev[0], c->ev[1]);
+            if (ms < best) { best = ms; c->batch_rc_threads = s.rc_threads; c->batch_tx_threads = s.idct_threads; }
+        }
+        CKB(cudaMemsetAsync(ctl + 1, 0, 4, st), "reset");
+        CKB(cudaMemsetAsync(ctl + 4, 0, (size_t)b->n_req * 4, st), "reset");
+    }
+    const BatchShape shape = {c->batch_rc_threads, c->batch_tx_threads};
+    // the graph bakes in every kernel parameter (buffers, archive tables) and the
+    // grid size: replay it only when all of them are unchanged
+    unsigned char key[512];
+    static_assert(sizeof(BatchJob) + sizeof(BatchShape) + sizeof(uint32_t) <= sizeof key, "graph key too small");
+    memset(key, 0, sizeof key);
+    memcpy(key, &J, sizeof J);
+    memcpy(key + sizeof J, &shape, sizeof shape);
+    memcpy(key + sizeof J + sizeof shape, &max_ua, sizeof max_ua);
+    if (!c->batch_graph || memcmp(key, c->batch_key, sizeof key) != 0) {
+        if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+        c->batch_graph = NULL;
+        cudaGraph_t g;
+        CKB(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture");
+        launch_batch(J, shape, g_dev.num_sms, max_ua, st);
+        CKB(cudaStreamEndCapture(st, &g), "graph capture");
+        cudaError_t e = cudaGraphInstantiate(&c->batch_graph, g, 0);
+        cudaGraphDestroy(g);
+        CKB(e, "graph instantiate");
+        memcpy(c->batch_key, key, sizeof key);
+    }
+    cudaEventRecord(c->ev[2], st);
+    CKB(cudaGraphLaunch(c->batch_graph, st), "graph launch");
+    cudaEventRecord(c->ev[3], st);
+    CKB(cudaMemcpyAsync(req_err, ctl + 4, (size_t)b->n_req * 4, cudaMemcpyDeviceToHost, st), "errors");
+    CKB(cudaStreamSynchronize(st), "batch decode");
+    CKB(cudaGetLastError(), "batch decode");
+    c->last_ms = vcd_elapsed(c->ev[2], c->ev[3]);
+    if (vcd_prof_on()) {
+        uint64_t out_bytes = 0;
+        for (uint32_t i = 0; i < b->n_req; ++i) {
+            const vcd_boxreq &r = b->reqs[i];
+            out_bytes += (uint64_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
+        }
+        vcd_prof_add("batch_decode", c->last_ms, 2, 0, out_bytes, b->n_ua);
+    }
+    if (host_out) {
+        void *pin;
+        CKB(vcd_pinned(c, out_total + 16, &pin), "batch staging");
+        CKB(cudaMemcpyAsync(pin, p_out, out_total, cudaMemcpyDeviceToHost, st), "batch copy-out");
+        CKB(cudaStreamSynchronize(st), "batch copy-out");
+        uint64_t o = 0;
+        for (uint32_t i = 0; i < b->n_req; ++i) {
+            const vcd_boxreq &r = b->reqs[i];
+            const uint64_t n = (uint64_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
+            if (host_out[i]) memcpy(host_out[i], (uint8_t *)pin + o, n);
+            o += (n + 15) & ~15ull;
+        }
+    }
+    return 0;
+}
+
+// Launch shape the autotuner chose for the calling thread (0 before the first batch).
+VC_API void vcg_batch_shape(int *rc_threads, int *transform_threads) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (rc_threads) *rc_threads = c ? c->batch_rc_threads : 0;
+    if (transform_threads) *transform_threads = c ? c->batch_tx_threads : 0;
+}

@@ -69,6 +69,7 @@ static void ctx_free(void *p) {
     for (int i = 0; i < VCD_NBUF; ++i)
         if (c->buf[i]) cudaFree(c->buf[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     if (c->stream) cudaStreamDestroy(c->stream);
     free(c);
 }
@@ -175,13 +176,6 @@ cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out) {
 }
 
 // ---------------------------------------------------------------- archive residency
-struct vcd_archive {
-    uint8_t *arc;       // archive bytes (+16 slack)
-    size_t len;
-    vcd_atom *atoms;    // all LODs
-    vcd_dq *dq;         // per LOD
-    int nlod;
-};
 
 extern "C" int vcd_upload_archive(vcd_archive **out, const uint8_t *buf, size_t len, const vcd_atom *atoms,
                                   uint64_t n_atoms, const vcd_dq *dq, int nlod) {

@@ -10,6 +10,8 @@ enum {
     VCD_BUF_CNT = 0, VCD_BUF_OFF, VCD_BUF_ENT, VCD_BUF_OUT,   // decode
     VCD_BUF_VOL, VCD_BUF_PYR, VCD_BUF_EENT, VCD_BUF_EMETA, VCD_BUF_LEN, VCD_BUF_POS, VCD_BUF_ARC,
     VCD_BUF_BEST, VCD_BUF_RED,
+    VCD_BUF_BUA, VCD_BUF_BDST, VCD_BUF_BREQ, VCD_BUF_BOFF, VCD_BUF_BCNT, VCD_BUF_BENT, VCD_BUF_BCTL, VCD_BUF_BOUT,
+    VCD_BUF_BPIN,
     VCD_NBUF
 };
 
@@ -21,6 +23,10 @@ struct vcd_ctx {
     size_t pinned_cap;
     cudaEvent_t ev[8];           // stage events of the last call on this thread
     double last_ms;              // device time of the last decode / encode call (start..end events)
+    // batched decode: autotuned launch shape and the CUDA graph of its launches
+    int batch_rc_threads, batch_tx_threads;
+    cudaGraphExec_t batch_graph;
+    unsigned char batch_key[512];   // kernel parameters + shape + grid capacity the graph was captured with
 };
 
 // Kernel statistics, accumulated while profiling is enabled (vcg_profile_enable).
@@ -28,6 +34,14 @@ int vcd_prof_on(void);
 void vcd_prof_add(const char *name, double ms, uint64_t launches, uint64_t bytes_read, uint64_t bytes_written,
                   uint64_t units);
 float vcd_elapsed(cudaEvent_t a, cudaEvent_t b);
+
+struct vcd_archive {
+    uint8_t *arc;       // archive bytes (+16 slack)
+    size_t len;
+    vcd_atom *atoms;    // all LODs
+    vcd_dq *dq;         // per LOD
+    int nlod;
+};
 
 struct vcd_device {
     int device, num_sms;

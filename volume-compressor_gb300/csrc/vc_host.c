@@ -441,6 +441,145 @@ VC_API vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev,
     return vcg_decode_region_device(a, lod, b, out_dev);
 }
 
+// ---------------------------------------------------------------------------
+// Batched region decode (include/vcg.h). Each request follows vc_decode_region
+// (src/vc/vc.c:1535-1555): its status is what that call would return, and a
+// request that meets a bad atom gets only the atoms before it (z, y, x order).
+// Across requests every distinct atom is decoded once.
+// ---------------------------------------------------------------------------
+typedef struct {
+    int32_t lod;
+    vc_box box;
+    uint8_t *out;
+} vcg_region_request;
+
+VC_API vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_request *reqs, int out_on_device,
+                                    vc_status *status) {
+    if (!a || (n && (!reqs || !status))) return VC_ERR_RANGE;
+    if (n == 0) return VC_OK;
+    if (make_resident(a) != 0) return VC_ERR_IO;
+    const uint64_t total_atoms = a->lod_base[a->nlod];
+    int32_t *uid = (int32_t *)malloc((total_atoms ? total_atoms : 1) * sizeof(int32_t));
+    vcd_boxreq *br = (vcd_boxreq *)calloc(n, sizeof(vcd_boxreq));
+    uint32_t *rmap = (uint32_t *)malloc(n * sizeof(uint32_t));   // device request slot -> request
+    size_t ref_cap = 1 << 16, nref = 0, ua_cap = 1 << 12, nua = 0;
+    uint32_t *ref_u = (uint32_t *)malloc(ref_cap * 4), *ref_r = (uint32_t *)malloc(ref_cap * 4);
+    vcd_uatom *ua = (vcd_uatom *)malloc(ua_cap * sizeof(vcd_uatom));
+    vc_status rc = VC_OK;
+    if (!uid || !br || !rmap || !ref_u || !ref_r || !ua) { rc = VC_ERR_OOM; goto done; }
+    memset(uid, 0xFF, total_atoms * sizeof(int32_t));
+    uint32_t nreq = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const vcg_region_request *q = &reqs[i];
+        vc_box b = q->box;
+        status[i] = VC_OK;
+        if (q->lod < 0 || q->lod >= a->nlod || !q->out) { status[i] = VC_ERR_RANGE; continue; }
+        vc_dims d = lod_dims_of(a->d0, q->lod);
+        if (b.x1 > d.nx || b.y1 > d.ny || b.z1 > d.nz || b.x0 >= b.x1 || b.y0 >= b.y1 || b.z0 >= b.z1) {
+            status[i] = VC_ERR_RANGE;
+            continue;
+        }
+        const uint32_t acx = (d.nx + 31) / 32, acy = (d.ny + 31) / 32;
+        if (!out_on_device) {
+            // a bad atom: only the atoms before it may reach the caller's buffer,
+            // which the plain path does exactly (rare: corrupt archives only)
+            int has_bad = 0;
+            for (uint32_t az = b.z0 / 32; az <= (b.z1 - 1) / 32 && !has_bad; ++az)
+                for (uint32_t ay = b.y0 / 32; ay <= (b.y1 - 1) / 32 && !has_bad; ++ay)
+                    for (uint32_t ax = b.x0 / 32; ax <= (b.x1 - 1) / 32; ++ax)
+                        if (a->atoms[a->lod_base[q->lod] + ((uint64_t)az * acy + ay) * acx + ax].kind == VCD_BAD) {
+                            has_bad = 1;
+                            break;
+                        }
+            if (has_bad) {
+                status[i] = decode_box(a, q->lod, b, q->out, NULL);
+                continue;
+            }
+        }
+        const uint32_t slot = nreq++;
+        rmap[slot] = i;
+        vcd_boxreq *r = &br[slot];
+        r->out = out_on_device ? q->out : NULL;
+        r->x0 = b.x0; r->y0 = b.y0; r->z0 = b.z0; r->x1 = b.x1; r->y1 = b.y1; r->z1 = b.z1;
+        r->lod = (uint32_t)q->lod;
+        int stop = 0;
+        for (uint32_t az = b.z0 / 32; az <= (b.z1 - 1) / 32 && !stop; ++az)
+            for (uint32_t ay = b.y0 / 32; ay <= (b.y1 - 1) / 32 && !stop; ++ay)
+                for (uint32_t ax = b.x0 / 32; ax <= (b.x1 - 1) / 32; ++ax) {
+                    const uint64_t g = a->lod_base[q->lod] + ((uint64_t)az * acy + ay) * acx + ax;
+                    if (a->atoms[g].kind == VCD_BAD) { status[i] = VC_ERR_FORMAT; stop = 1; break; }
+                    if (uid[g] < 0) {
+                        if (nua == ua_cap) {
+                            ua_cap *= 2;
+                            vcd_uatom *t = (vcd_uatom *)realloc(ua, ua_cap * sizeof(vcd_uatom));
+                            if (!t) { rc = VC_ERR_OOM; goto done; }
+                            ua = t;
+                        }
+                        uid[g] = (int32_t)nua;
+                        vcd_uatom *u = &ua[nua++];
+                        memset(u, 0, sizeof *u);
+                        u->idx = g; u->lod = (uint32_t)q->lod; u->az = az; u->ay = ay; u->ax = ax;
+                    }
+                    if (nref == ref_cap) {
+                        ref_cap *= 2;
+                        uint32_t *t1 = (uint32_t *)realloc(ref_u, ref_cap * 4), *t2 = t1 ? (uint32_t *)realloc(ref_r, ref_cap * 4) : NULL;
+                        if (t1) ref_u = t1;
+                        if (t2) ref_r = t2;
+                        if (!t1 || !t2) { rc = VC_ERR_OOM; goto done; }
+                    }
+                    ref_u[nref] = (uint32_t)uid[g];
+                    ref_r[nref++] = slot;
+                    ++ua[uid[g]].dst_end;   // count for now
+                }
+    }
+    if (nreq) {
+        // CSR of destinations per distinct atom; list offsets by capacity
+        uint32_t *dst = (uint32_t *)malloc((nref ? nref : 1) * 4);
+        uint64_t *off = (uint64_t *)malloc((nua ? nua : 1) * 8);
+        if (!dst || !off) { free(dst); free(off); rc = VC_ERR_OOM; goto done; }
+        uint32_t acc = 0;
+        uint64_t cap = 0;
+        for (size_t u = 0; u < nua; ++u) {
+            const uint32_t c = ua[u].dst_end;
+            ua[u].dst_begin = acc;
+            ua[u].dst_end = acc;
+            acc += c;
+            off[u] = cap;
+            const vcd_atom *t = &a->atoms[ua[u].idx];
+            if (t->kind == VCD_PRESENT) cap += entry_cap(t);
+        }
+        for (size_t k = 0; k < nref; ++k) dst[ua[ref_u[k]].dst_end++] = ref_r[k];
+        vcd_batch bt = {nreq, (uint32_t)nua, (uint32_t)nref, br, ua, dst, off, cap};
+        uint8_t **hout = NULL;
+        if (!out_on_device) {
+            hout = (uint8_t **)malloc(nreq * sizeof(uint8_t *));
+            if (!hout) { free(dst); free(off); rc = VC_ERR_OOM; goto done; }
+            for (uint32_t s = 0; s < nreq; ++s) hout[s] = reqs[rmap[s]].out;
+        }
+        uint32_t *err = (uint32_t *)calloc(nreq, 4);
+        int drc = err ? vcd_decode_batch(a->dev, &bt, hout, err) : VC_ERR_OOM;
+        if (drc) {
+            report("batched decode failed: %s", vcd_last_error());
+            rc = (vc_status)drc;
+        } else {
+            for (uint32_t s = 0; s < nreq; ++s)
+                if (err[s]) status[rmap[s]] = VC_ERR_FORMAT;
+        }
+        free(err);
+        free(hout);
+        free(dst);
+        free(off);
+    }
+done:
+    free(uid);
+    free(br);
+    free(rmap);
+    free(ref_u);
+    free(ref_r);
+    free(ua);
+    return rc;
+}
+
 VC_API vc_status vcg_make_resident(vc_archive *a) {
     if (!a) return VC_ERR_RANGE;
     return make_resident(a) == 0 ? VC_OK : VC_ERR_IO;

@@ -64,6 +64,27 @@ typedef struct {
     int lod;
 } vcd_region;
 
+// Batched region decode, built on the host.
+typedef struct {         // one request box (device view)
+    uint8_t *out;        // box raster, device memory (filled in by the device layer for host outputs)
+    uint32_t x0, y0, z0, x1, y1, z1;
+    uint32_t lod, rsv;
+} vcd_boxreq;
+typedef struct {         // one distinct atom of a batch
+    uint64_t idx;        // index in the archive's atom table (all LODs)
+    uint32_t lod, az, ay, ax;
+    uint32_t dst_begin, dst_end;   // the requests it feeds: dst[dst_begin .. dst_end)
+    uint32_t rsv;
+} vcd_uatom;
+typedef struct {
+    uint32_t n_req, n_ua, n_dst;
+    vcd_boxreq *reqs;
+    const vcd_uatom *ua;
+    const uint32_t *dst;
+    const uint64_t *ent_off;  // per distinct atom
+    uint64_t cap_total;       // list entries in total
+} vcd_batch;
+
 typedef struct vcd_archive vcd_archive;   // device residency of one archive
 
 // ---- device layer (vc_device.cu) ------------------------------------------
@@ -76,6 +97,11 @@ void vcd_free_archive(vcd_archive *d);
 // the host buffer out_host (box raster); returns 0 or a vc_status
 int  vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *out_dev, uint8_t *out_host,
                        size_t out_bytes);
+
+// Batched decode. Outputs: reqs[i].out (device) when host_out is NULL, else
+// host_out[i] (the device layer stages through its own buffer). req_err[i] is
+// set to 1 for requests that met a malformed stream.
+int  vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *const *host_out, uint32_t *req_err);
 
 // Encode: volume (device or host) -> canonical archive (host malloc).
 typedef struct {

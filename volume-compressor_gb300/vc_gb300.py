@@ -22,7 +22,7 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
               "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q", "vcg_decode_atoms_noalloc",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
                "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_last_error", "vcg_profile_enable",
                "vcg_profile_read", "vcg_last_call_ms"]
@@ -34,6 +34,16 @@ class Dims(ctypes.Structure):
 
 class Box(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint32) for n in ("x0", "y0", "z0", "x1", "y1", "z1")]
+
+
+class RegionRequest(ctypes.Structure):
+    _fields_ = [("lod", ctypes.c_int32), ("box", Box), ("out", ctypes.c_void_p)]
+
+
+def batch_shape():
+    a, b = ctypes.c_int(), ctypes.c_int()
+    lib().vcg_batch_shape(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
 
 
 P = ctypes.c_void_p
@@ -89,6 +99,8 @@ def lib():
         L.vcg_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
         L.vcg_last_error.restype = ctypes.c_char_p
         L.vcg_decode_atoms_noalloc.argtypes = [P, ctypes.c_size_t, P, P, ctypes.c_uint32, ctypes.c_float, P]
+        L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
+        L.vcg_batch_shape.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.vcg_profile_enable.argtypes = [ctypes.c_int]
         L.vcg_profile_read.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.vcg_last_call_ms.restype = ctypes.c_double
@@ -285,6 +297,18 @@ class Archive:
 
     def decode_region_device(self, lod, box, dbuf):
         return lib().vcg_decode_region_device(self.h, lod, Box(*box), dbuf.ptr)
+
+    def decode_regions(self, reqs, outs, on_device=False):
+        """vcg_decode_regions: reqs = [(lod, (x0,y0,z0,x1,y1,z1))], outs = numpy arrays (host)
+        or DeviceBuffers (device). Returns (call status, per-request statuses)."""
+        arr = (RegionRequest * len(reqs))()
+        for i, ((lod, box), o) in enumerate(zip(reqs, outs)):
+            arr[i].lod = lod
+            arr[i].box = Box(*box)
+            arr[i].out = o.ptr if on_device else o.ctypes.data
+        st = np.zeros(len(reqs), np.int32)
+        s = lib().vcg_decode_regions(self.h, len(reqs), arr, 1 if on_device else 0, ptr(st))
+        return s, st
 
     def coverage(self, lod, az, ay, ax):
         return lib().vc_atom_coverage(self.h, lod, az, ay, ax)
