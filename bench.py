@@ -44,6 +44,7 @@ def args_parse():
     p.add_argument("--target", type=float, default=10.0)
     p.add_argument("--regions", type=int, default=200)
     p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched-region measurement")
+    p.add_argument("--no-served", action="store_true", help="skip the config-5 served-decode measurement")
     return p.parse_args()
 
 
@@ -269,6 +270,172 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             "bit_exact_sample": ok, "plain_sample": plain_sample}
 
 
+def served_mix(a, rng, n):
+    """Request mix of the served-decode workload: 70% single 32^3 atoms at LOD0,
+    25% boxes with edges U[64,128] at LOD 0-1, 5% 512^3 boxes at LOD2."""
+    reqs = []
+    for _ in range(n):
+        u = rng.random()
+        if u < 0.70:
+            d = a.lod_dims(0)[1]
+            o = [32 * int(rng.integers(0, (d[k] + 31) // 32)) for k in range(3)]
+            e = [min(32, d[k] - o[k]) for k in range(3)]
+            lod = 0
+        elif u < 0.95:
+            lod = int(rng.integers(0, 2))
+            d = a.lod_dims(lod)[1]
+            e = [int(min(rng.integers(64, 129), d[k])) for k in range(3)]
+            o = [int(rng.integers(0, d[k] - e[k] + 1)) for k in range(3)]
+        else:
+            lod = 2
+            d = a.lod_dims(2)[1]
+            e = [min(512, d[k]) for k in range(3)]
+            o = [int(rng.integers(0, d[k] - e[k] + 1)) for k in range(3)]
+        reqs.append((lod, (o[0], o[1], o[2], o[0] + e[0], o[1] + e[1], o[2] + e[2])))
+    return reqs
+
+
+def _box_bytes(b):
+    return (b[3] - b[0]) * (b[4] - b[1]) * (b[5] - b[2])
+
+
+def _pace(t0, arrival):
+    while True:
+        dt = t0 + arrival - time.perf_counter()
+        if dt <= 0:
+            return
+        time.sleep(dt if dt > 2e-3 else 0)
+
+
+def _serve_stream(a, reqs, arrivals, outs, server_cfg):
+    """One Poisson stream through the decode server. Returns per-request
+    latencies (µs, submit to completion) and the wall time first arrival -> last
+    completion."""
+    import numpy as np
+    srv = a.server(**server_cfg)
+    tix = [None] * len(reqs)
+    lat = np.zeros(len(reqs))
+    status = np.zeros(len(reqs), np.int32)
+    ready = threading.Semaphore(0)
+
+    def waiter():
+        for i in range(len(reqs)):
+            ready.acquire()
+            status[i], lat[i] = srv.wait(tix[i])
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    for i, (lod, box) in enumerate(reqs):
+        _pace(t0, arrivals[i])
+        tix[i] = srv.submit(lod, box, outs[i])
+        ready.release()
+    th.join()
+    wall = time.perf_counter() - t0
+    batches, done = srv.stats()
+    srv.close()
+    assert not status.any(), f"server statuses {np.unique(status)}"
+    return lat, wall, done / max(1, batches)
+
+
+def _plain_stream(a, reqs, arrivals, outs, workers):
+    """The same stream through the plain per-request path: `workers` threads take
+    requests in arrival order and call vc_decode_region one at a time."""
+    import numpy as np
+    lat = np.zeros(len(reqs))
+    status = np.zeros(len(reqs), np.int32)
+    nxt = [0]
+    mu = threading.Lock()
+    t0 = time.perf_counter()
+
+    def run():
+        while True:
+            with mu:
+                i = nxt[0]
+                nxt[0] += 1
+            if i >= len(reqs):
+                return
+            _pace(t0, arrivals[i])
+            status[i] = a.decode_region(reqs[i][0], reqs[i][1], outs[i])[0]
+            lat[i] = (time.perf_counter() - t0 - arrivals[i]) * 1e6
+    th = [threading.Thread(target=run) for _ in range(workers)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    wall = time.perf_counter() - t0
+    assert not status.any(), f"plain statuses {np.unique(status)}"
+    return lat, wall
+
+
+def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000, verify_n=400):
+    """Served decode: 2048^3 volume at target_ratio 20 resident in HBM; Poisson
+    request streams at swept rates through the continuous-batching server
+    (vcg_server_*) and through the plain per-request path (vc_decode_region on
+    as many host threads as the server has workers). Outputs are host memory;
+    large-box outputs rotate through a pool in the timed streams, and a separate
+    stream of verify_n requests with distinct outputs is checked byte for byte
+    against vc_decode_region."""
+    import numpy as np
+    import vc_gb300 as vc
+    n = 2048
+    dv = vc.synth_device(n, n, n, vc.config_seed(5))
+    s, data, q0 = vc.encode_device(dv, (n, n, n), 20.0)
+    assert s == 0, vc.last_error()
+    dv.free()
+    a = vc.Archive(data)
+    assert a.make_resident() == 0
+    cfg = {"device_budget": 2 << 30, "max_batch": 1024, "workers": 2}
+    rng = np.random.default_rng(0x5E5E)
+    warm = served_mix(a, rng, 64)   # first batches tune the launch shape and build graphs
+    wo = [np.empty(_box_bytes(b), np.uint8) for _, b in warm]
+    _serve_stream(a, warm, np.zeros(len(warm)), wo, cfg)
+    big_pool = [np.empty(512 ** 3, np.uint8) for _ in range(8)]
+    sweep = []
+    for rate in rates:
+        m = int(min(max_requests, max(200, rate * seconds)))
+        reqs = served_mix(a, rng, m)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, m))
+        outs, k = [], 0
+        for _, b in reqs:
+            nb = _box_bytes(b)
+            if nb == 512 ** 3:
+                outs.append(big_pool[k % len(big_pool)])
+                k += 1
+            else:
+                outs.append(np.empty(nb, np.uint8))
+        total = sum(_box_bytes(b) for _, b in reqs)
+        row = {"offered_rps": rate, "requests": m, "out_bytes": total}
+        for name, fn in (("server", lambda: _serve_stream(a, reqs, arrivals, outs, cfg)),
+                         ("plain", lambda: _plain_stream(a, reqs, arrivals, outs, cfg["workers"]))):
+            r = fn()
+            lat, wall = r[0], r[1]
+            row[name] = {"p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
+                         "GBps": total / wall / 1e9, "achieved_rps": m / wall}
+            if name == "server":
+                row[name]["mean_batch"] = r[2]
+        sweep.append(row)
+    # bit-exactness: distinct outputs, highest rate, every request checked
+    reqs = served_mix(a, rng, verify_n)
+    arrivals = np.cumsum(rng.exponential(1.0 / rates[-1], verify_n))
+    outs = [np.empty(_box_bytes(b), np.uint8) for _, b in reqs]
+    _serve_stream(a, reqs, arrivals, outs, cfg)
+    ok, ref_cache = True, {}
+    for (lod, box), o in zip(reqs, outs):
+        key = (lod, box)
+        if key not in ref_cache:
+            ref = np.empty(_box_bytes(box), np.uint8)
+            assert a.decode_region(lod, box, ref)[0] == 0
+            ref_cache[key] = ref if _box_bytes(box) == 512 ** 3 else None
+        else:
+            ref = ref_cache[key]
+        ok = ok and bool(np.array_equal(o, ref))
+    a.close()
+    return {"workload": "2048^3 at target_ratio 20 resident in HBM; Poisson arrivals; 70% 32^3 atoms LOD0, "
+                        "25% boxes U[64,128]^3 LOD0-1, 5% 512^3 LOD2; host outputs",
+            "q0": q0, "archive_bytes": len(data), "server": cfg, "plain_threads": cfg["workers"],
+            "sweep": sweep, "bit_exact_all_outputs": ok, "verified_requests": verify_n}
+
+
 # ---------------------------------------------------------------- arms
 def reference_arm(args, dist):
     if dist.rank != 0:
@@ -416,6 +583,13 @@ def gb300_arm(args, dist):
         out.free()
         flush.free()
         batched = config4_batched()
+    served = None
+    if dist.rank == 0 and not args.no_served:
+        if args.no_batched:
+            arc.close()
+            out.free()
+            flush.free()
+        served = config5_served()
     if dist.rank != 0:
         return
     line = {
@@ -444,6 +618,8 @@ def gb300_arm(args, dist):
         line["cpu_baseline"] = cpu
     if batched:
         line["batched_regions"] = batched
+    if served:
+        line["served_regions"] = served
     print(json.dumps(line), flush=True)
 
 

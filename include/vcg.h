@@ -25,8 +25,8 @@ vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev, vc_dim
 // vc_decode_region would return for request i, and outputs follow its rules
 // (a request that meets a bad atom gets only the atoms before it, z-y-x order).
 // out_on_device != 0: every out is device memory; else host memory. The launch
-// shape is autotuned on the calling thread's first batch; later batches replay
-// one CUDA graph.
+// shape is autotuned on the process's first batch; a thread's later batches
+// replay one CUDA graph while the batch buffers keep their addresses.
 typedef struct {
     int32_t lod;
     vc_box box;
@@ -34,9 +34,26 @@ typedef struct {
 } vcg_region_request;
 vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_request *reqs, int out_on_device,
                              vc_status *status);
-// Launch shape chosen by the autotuner for the calling thread (0 before the
-// first batch): range-decoder CTA size and transform CTA size (32 x warps per atom).
+// Launch shape the calling thread uses (0 before its first batch): range-decoder
+// CTA size and transform CTA size (32 x warps per atom).
 void vcg_batch_shape(int *rc_threads, int *transform_threads);
+
+// Decode server: continuous batching against one resident archive. Requests
+// queue with vcg_server_submit; `workers` threads (each with its own stream)
+// take waiting requests in arrival order, as many as fit `device_budget` bytes
+// (box output + list scratch) and `max_batch`, decode them with
+// vcg_decode_regions and release their memory; requests that arrive while
+// batches run join the next batch, and batches of different workers overlap on
+// the device. Results and statuses equal vc_decode_region's for each request.
+typedef struct vcg_server vcg_server;
+vcg_server *vcg_server_create(vc_archive *a, uint64_t device_budget, uint32_t max_batch, int workers);
+// out: host memory of the box's size, valid until the ticket completes; returns a ticket >= 0, or -1
+int64_t vcg_server_submit(vcg_server *s, int lod, vc_box box, uint8_t *out);
+// blocks until the ticket is done; latency_us (optional) = submit-to-completion time
+vc_status vcg_server_wait(vcg_server *s, int64_t ticket, double *latency_us);
+void vcg_server_stats(vcg_server *s, uint64_t *batches, uint64_t *requests);
+// finishes all queued requests, then stops the workers
+void vcg_server_destroy(vcg_server *s);
 
 // Resolve the archive's atom table and copy archive + table into device
 // memory now (otherwise done on the first decode).

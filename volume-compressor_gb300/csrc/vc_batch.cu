@@ -2,8 +2,9 @@
 // atoms, their destination lists, the request boxes, list offsets) into
 // grow-only device buffers, then replay one CUDA graph of the persistent
 // range-decode + transform launches. The launch shape (range-decoder CTA size,
-// transform CTA size) is picked once per host thread by timing every candidate
-// on the first batch (all candidates produce identical bytes).
+// transform CTA size) is picked once per process by timing every candidate on
+// the first batch (all candidates produce identical bytes); threads that start
+// later take the tuned shape.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -29,6 +30,9 @@ static const BatchShape kShapes[] = {{64, 256}, {128, 256}, {256, 256}, {64, 512
     } while (0)
 
 static size_t cap_of(const vcd_ctx *c, int slot) { return c->cap[slot]; }
+
+// tuned shape shared by all threads: rc_threads << 16 | transform threads (0 = not yet)
+static int g_tuned_shape = 0;
 
 extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *const *host_out, uint32_t *req_err) {
     vcd_ctx *c = vcd_thread_ctx();
@@ -85,7 +89,11 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
     // capacity in distinct atoms the range-decode grid must cover (the buffer's)
     const uint32_t max_ua = (uint32_t)((cap_of(c, VCD_BUF_BUA) - 64) / sizeof(vcd_uatom));
 
-    if (!c->batch_rc_threads) {   // autotune on this first batch
+    if (!c->batch_rc_threads) {
+        const int t = __atomic_load_n(&g_tuned_shape, __ATOMIC_ACQUIRE);
+        if (t) { c->batch_rc_threads = t >> 16; c->batch_tx_threads = t & 0xFFFF; }
+    }
+    if (!c->batch_rc_threads) {   // autotune on the process's first batch
         float best = 1e30f;
         for (const BatchShape &s : kShapes) {
             CKB(cudaMemsetAsync(ctl + 1, 0, 4, st), "reset");
@@ -99,6 +107,7 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
         }
         CKB(cudaMemsetAsync(ctl + 1, 0, 4, st), "reset");
         CKB(cudaMemsetAsync(ctl + 4, 0, (size_t)b->n_req * 4, st), "reset");
+        __atomic_store_n(&g_tuned_shape, c->batch_rc_threads << 16 | c->batch_tx_threads, __ATOMIC_RELEASE);
     }
     const BatchShape shape = {c->batch_rc_threads, c->batch_tx_threads};
     // the graph bakes in every kernel parameter (buffers, archive tables) and the
@@ -152,7 +161,7 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
     return 0;
 }
 
-// Launch shape the autotuner chose for the calling thread (0 before the first batch).
+// Launch shape the calling thread uses (0 before its first batch).
 VC_API void vcg_batch_shape(int *rc_threads, int *transform_threads) {
     vcd_ctx *c = vcd_thread_ctx();
     if (rc_threads) *rc_threads = c ? c->batch_rc_threads : 0;

@@ -10,7 +10,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "../../include/vc.h"
+#include "../../include/vcg.h"
 #include "vc_internal.h"
 #include "vc_release_tables.h"
 
@@ -447,11 +447,6 @@ VC_API vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev,
 // request that meets a bad atom gets only the atoms before it (z, y, x order).
 // Across requests every distinct atom is decoded once.
 // ---------------------------------------------------------------------------
-typedef struct {
-    int32_t lod;
-    vc_box box;
-    uint8_t *out;
-} vcg_region_request;
 
 VC_API vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_request *reqs, int out_on_device,
                                     vc_status *status) {

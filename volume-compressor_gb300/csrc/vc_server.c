@@ -1,0 +1,193 @@
+// Decode server: continuous batching of vc_decode_region requests against one
+// archive kept resident in device memory.
+//
+// Requests are queued by vcg_server_submit and decoded by a small pool of
+// worker threads, each with its own CUDA stream. A worker takes, in arrival
+// order, as many waiting requests as the shared device-memory budget and its
+// batch limit allow, decodes them in one batched pass (each distinct atom once,
+// cropped into every box; vcg_decode_regions) and releases their budget.
+// Requests that arrive while batches are on the GPU join the next batch of
+// whichever worker frees up first, so batches from different workers overlap on
+// the device. Each result is exactly what vc_decode_region returns for that
+// request alone.
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "../../include/vcg.h"
+
+#define VC_API __attribute__((visibility("default")))
+
+
+typedef struct {
+    vcg_region_request req;
+    uint64_t cost;          // device bytes the request holds while decoding
+    double t_submit, t_done;
+    vc_status status;
+    int state;              // 0 queued, 1 running, 2 done
+} srv_req;
+
+typedef struct vcg_server {
+    vc_archive *a;
+    uint64_t budget, in_use;
+    uint32_t max_batch;
+    int nworkers, stop;
+    pthread_t th[8];
+    pthread_mutex_t mu;
+    pthread_cond_t work_cv, done_cv;
+    srv_req *reqs;          // ticket -> request (grows)
+    uint64_t cap, n;        // tickets issued
+    uint64_t head;          // first ticket not yet taken by a worker
+    uint64_t batches, batched_reqs;
+} vcg_server;
+
+static double now_us(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec * 1e6 + ts.tv_nsec * 1e-3;
+}
+
+// Device bytes a request holds while in a batch: its staged output plus list
+// scratch for the atoms it touches (bounded by 32 KiB per atom on average).
+static uint64_t cost_of(const vc_box *b) {
+    uint64_t vox = (uint64_t)(b->x1 - b->x0) * (b->y1 - b->y0) * (b->z1 - b->z0);
+    uint64_t atoms = (uint64_t)((b->x1 - 1) / 32 - b->x0 / 32 + 1) * ((b->y1 - 1) / 32 - b->y0 / 32 + 1) *
+                     ((b->z1 - 1) / 32 - b->z0 / 32 + 1);
+    return vox + atoms * 32768ull;
+}
+
+static void *worker(void *arg) {
+    vcg_server *s = (vcg_server *)arg;
+    vcg_region_request *batch = (vcg_region_request *)malloc(s->max_batch * sizeof(vcg_region_request));
+    vc_status *st = (vc_status *)malloc(s->max_batch * sizeof(vc_status));
+    uint64_t *tix = (uint64_t *)malloc(s->max_batch * sizeof(uint64_t));
+    pthread_mutex_lock(&s->mu);
+    for (;;) {
+        while (!s->stop && s->head == s->n) pthread_cond_wait(&s->work_cv, &s->mu);
+        if (s->stop && s->head == s->n) break;
+        // admit in arrival order while memory and the batch limit allow; a
+        // request larger than the whole budget runs alone
+        uint32_t k = 0;
+        uint64_t take = 0;
+        while (s->head < s->n && k < s->max_batch) {
+            srv_req *r = &s->reqs[s->head];
+            if (s->in_use + take + r->cost > s->budget && (k > 0 || s->in_use > 0)) break;
+            r->state = 1;
+            batch[k] = r->req;
+            tix[k] = s->head;
+            take += r->cost;
+            ++k;
+            ++s->head;
+        }
+        if (k == 0) {   // waiting for memory held by other workers
+            pthread_cond_wait(&s->done_cv, &s->mu);
+            continue;
+        }
+        s->in_use += take;
+        pthread_mutex_unlock(&s->mu);
+        vc_status rc = vcg_decode_regions(s->a, k, batch, 0, st);
+        double t = now_us();
+        pthread_mutex_lock(&s->mu);
+        for (uint32_t i = 0; i < k; ++i) {
+            srv_req *r = &s->reqs[tix[i]];
+            r->status = rc != VC_OK ? rc : st[i];
+            r->t_done = t;
+            r->state = 2;
+        }
+        s->in_use -= take;
+        s->batches++;
+        s->batched_reqs += k;
+        pthread_cond_broadcast(&s->done_cv);
+        pthread_cond_broadcast(&s->work_cv);
+    }
+    pthread_mutex_unlock(&s->mu);
+    free(batch);
+    free(st);
+    free(tix);
+    return NULL;
+}
+
+// device_budget: device bytes that requests in flight may hold (outputs plus
+// list scratch); max_batch: requests per batch; workers: 1..8 batches in flight.
+VC_API vcg_server *vcg_server_create(vc_archive *a, uint64_t device_budget, uint32_t max_batch, int workers) {
+    if (!a || !device_budget || !max_batch || workers < 1 || workers > 8) return NULL;
+    vcg_server *s = (vcg_server *)calloc(1, sizeof *s);
+    if (!s) return NULL;
+    s->a = a;
+    s->budget = device_budget;
+    s->max_batch = max_batch;
+    s->cap = 1024;
+    s->reqs = (srv_req *)calloc(s->cap, sizeof(srv_req));
+    if (!s->reqs) { free(s); return NULL; }
+    pthread_mutex_init(&s->mu, NULL);
+    pthread_cond_init(&s->work_cv, NULL);
+    pthread_cond_init(&s->done_cv, NULL);
+    for (int i = 0; i < workers; ++i) {
+        if (pthread_create(&s->th[i], NULL, worker, s) != 0) break;
+        s->nworkers++;
+    }
+    if (!s->nworkers) { free(s->reqs); free(s); return NULL; }
+    return s;
+}
+
+// Queue one request; returns its ticket (>= 0) or -1. out is host memory of the
+// box's size and must stay valid until the ticket completes.
+VC_API int64_t vcg_server_submit(vcg_server *s, int lod, vc_box box, uint8_t *out) {
+    if (!s) return -1;
+    pthread_mutex_lock(&s->mu);
+    if (s->n == s->cap) {
+        srv_req *t = (srv_req *)realloc(s->reqs, 2 * s->cap * sizeof(srv_req));
+        if (!t) { pthread_mutex_unlock(&s->mu); return -1; }
+        s->reqs = t;
+        s->cap *= 2;
+    }
+    srv_req *r = &s->reqs[s->n];
+    memset(r, 0, sizeof *r);
+    r->req.lod = lod;
+    r->req.box = box;
+    r->req.out = out;
+    r->cost = box.x1 > box.x0 && box.y1 > box.y0 && box.z1 > box.z0 ? cost_of(&box) : 0;
+    r->t_submit = now_us();
+    int64_t ticket = (int64_t)s->n++;
+    pthread_cond_signal(&s->work_cv);
+    pthread_mutex_unlock(&s->mu);
+    return ticket;
+}
+
+// Block until the ticket is decoded; returns its status (vc_decode_region's),
+// and the submit-to-completion latency in microseconds.
+VC_API vc_status vcg_server_wait(vcg_server *s, int64_t ticket, double *latency_us) {
+    if (!s || ticket < 0) return VC_ERR_RANGE;
+    pthread_mutex_lock(&s->mu);
+    if ((uint64_t)ticket >= s->n) { pthread_mutex_unlock(&s->mu); return VC_ERR_RANGE; }
+    while (s->reqs[ticket].state != 2) pthread_cond_wait(&s->done_cv, &s->mu);
+    vc_status st = s->reqs[ticket].status;
+    if (latency_us) *latency_us = s->reqs[ticket].t_done - s->reqs[ticket].t_submit;
+    pthread_mutex_unlock(&s->mu);
+    return st;
+}
+
+// Batches run and requests they carried so far.
+VC_API void vcg_server_stats(vcg_server *s, uint64_t *batches, uint64_t *requests) {
+    if (!s) return;
+    pthread_mutex_lock(&s->mu);
+    if (batches) *batches = s->batches;
+    if (requests) *requests = s->batched_reqs;
+    pthread_mutex_unlock(&s->mu);
+}
+
+// Finishes every queued request, then stops the workers.
+VC_API void vcg_server_destroy(vcg_server *s) {
+    if (!s) return;
+    pthread_mutex_lock(&s->mu);
+    s->stop = 1;
+    pthread_cond_broadcast(&s->work_cv);
+    pthread_mutex_unlock(&s->mu);
+    for (int i = 0; i < s->nworkers; ++i) pthread_join(s->th[i], NULL);
+    pthread_mutex_destroy(&s->mu);
+    pthread_cond_destroy(&s->work_cv);
+    pthread_cond_destroy(&s->done_cv);
+    free(s->reqs);
+    free(s);
+}

@@ -23,6 +23,8 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
                "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape",
+               "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
+               "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
                "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_last_error", "vcg_profile_enable",
                "vcg_profile_read", "vcg_last_call_ms"]
@@ -38,6 +40,48 @@ class Box(ctypes.Structure):
 
 class RegionRequest(ctypes.Structure):
     _fields_ = [("lod", ctypes.c_int32), ("box", Box), ("out", ctypes.c_void_p)]
+
+
+class Server:
+    """vcg_server_*: continuous-batching decode server over one Archive. submit()
+    keeps the output array alive until wait() returns its ticket."""
+
+    def __init__(self, archive, device_budget, max_batch, workers):
+        self.archive = archive
+        self.h = lib().vcg_server_create(archive.h, device_budget, max_batch, workers)
+        if not self.h:
+            raise RuntimeError("vcg_server_create failed")
+        self._outs = {}
+
+    def submit(self, lod, box, out):
+        t = lib().vcg_server_submit(self.h, lod, Box(*box), out.ctypes.data)
+        if t >= 0:
+            self._outs[t] = out
+        return t
+
+    def wait(self, ticket):
+        """Returns (status, latency in microseconds)."""
+        lat = ctypes.c_double()
+        s = lib().vcg_server_wait(self.h, ticket, ctypes.byref(lat))
+        self._outs.pop(ticket, None)
+        return s, lat.value
+
+    def stats(self):
+        b, r = ctypes.c_uint64(), ctypes.c_uint64()
+        lib().vcg_server_stats(self.h, ctypes.byref(b), ctypes.byref(r))
+        return b.value, r.value
+
+    def close(self):
+        if self.h:
+            lib().vcg_server_destroy(self.h)
+            self.h = None
+            self._outs.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def batch_shape():
@@ -101,6 +145,13 @@ def lib():
         L.vcg_decode_atoms_noalloc.argtypes = [P, ctypes.c_size_t, P, P, ctypes.c_uint32, ctypes.c_float, P]
         L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
         L.vcg_batch_shape.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        L.vcg_server_create.restype = P
+        L.vcg_server_create.argtypes = [P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int]
+        L.vcg_server_submit.restype = ctypes.c_int64
+        L.vcg_server_submit.argtypes = [P, ctypes.c_int, Box, P]
+        L.vcg_server_wait.argtypes = [P, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+        L.vcg_server_stats.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        L.vcg_server_destroy.argtypes = [P]
         L.vcg_profile_enable.argtypes = [ctypes.c_int]
         L.vcg_profile_read.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.vcg_last_call_ms.restype = ctypes.c_double
@@ -309,6 +360,9 @@ class Archive:
         st = np.zeros(len(reqs), np.int32)
         s = lib().vcg_decode_regions(self.h, len(reqs), arr, 1 if on_device else 0, ptr(st))
         return s, st
+
+    def server(self, device_budget=1 << 30, max_batch=4096, workers=2):
+        return Server(self, device_budget, max_batch, workers)
 
     def coverage(self, lod, az, ay, ax):
         return lib().vc_atom_coverage(self.h, lod, az, ay, ax)
