@@ -128,6 +128,18 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def dram_traffic(kernel, units):
+    """DRAM bytes (read + write) of one launch of `kernel` processing `units`
+    atoms, scaled from the per-atom figure of an ncu capture committed in
+    profiles/dram_traffic.json; None when there is none."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            per_atom = json.load(f)["bytes_per_atom"][kernel]
+        return per_atom * units
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -265,7 +277,7 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             "batched_ms": batch_ms, "batched_GBps": batch_gbps, "batched_us_per_request": batch_ms * 1e3 / n_boxes,
             "plain_GBps": plain_gbps, "plain_p50_us": plain_ms[len(plain_ms) // 2] * 1e3,
             "plain_p99_us": plain_ms[min(len(plain_ms) - 1, int(0.99 * len(plain_ms)))] * 1e3,
-            "speedup_vs_plain": batch_gbps / plain_gbps, "autotuned_shape": {"rc_threads": shape[0],
+            "speedup_vs_plain": batch_gbps / plain_gbps, "autotuned_shape": {"rc_scalar_warps": shape[0],
                                                                             "transform_threads": shape[1]},
             "bit_exact_sample": ok, "plain_sample": plain_sample}
 
@@ -603,14 +615,16 @@ def gb300_arm(args, dist):
         "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches,
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "frac": achieved / peak, "traffic": dram_traffic(dom, st_["units"] / max(1, st_["launches"])),
+                     "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
         "stages": {k: {"ms_per_step": v["ms"] / args.steps, "GBps_algorithmic":
                        (v["bytes_read"] + v["bytes_written"]) / max(1e-9, v["ms"] / 1e3) / 1e9}
                    for k, v in stats.items()},
         "encode_GBps": nbytes / (statistics.median(enc_ms) / 1e3) / 1e9,
         "encode_with_rate_control_GBps": nbytes / (enc_full_ms / 1e3) / 1e9,
-        "region_p50_us": lat[len(lat) // 2], "region_p99_us": lat[min(len(lat) - 1, int(len(lat) * 0.99))],
+        "region_p50_us": lat[len(lat) // 2] if lat else None,
+        "region_p99_us": lat[min(len(lat) - 1, int(len(lat) * 0.99))] if lat else None,
         "bit_exact": {"archive_vs_reference": bit_exact_archive, "lod0_vs_reference": lod0_ok},
         "clocks": clk,
     }

@@ -35,8 +35,19 @@ typedef struct {
 vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_request *reqs, int out_on_device,
                              vc_status *status);
 // Launch shape the calling thread uses (0 before its first batch): range-decoder
-// CTA size and transform CTA size (32 x warps per atom).
-void vcg_batch_shape(int *rc_threads, int *transform_threads);
+// policy (warps per SM sub-partition that decode one atom each before atoms
+// share warps in lockstep; see vcg_set_rc_scalar_warps) and transform CTA size
+// (32 x warps per atom).
+void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads);
+
+// Range-decoder policy of vc_decode_region / vc_decode_lod / vc_decode_atom and
+// the device-output variants (process-wide; results do not depend on it). A
+// warp that decodes one atom has the lowest latency per atom; warps of 2..32
+// atoms decoded in lockstep have the highest throughput. Atoms are decoded one
+// per warp while that makes at most w warps per SM sub-partition (4 per SM),
+// else in warps of the smallest power of two that keeps to about one warp per
+// sub-partition. w <= 0 restores the default (4).
+void vcg_set_rc_scalar_warps(int w);
 
 // Decode server: continuous batching against one resident archive. Requests
 // queue with vcg_server_submit; `workers` threads (each with its own stream)

@@ -37,11 +37,9 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
     __syncthreads();
     if (c & kEntOverflow) {
         // slow path for streams whose list exceeded its capacity
-        if (tid == 0) {
-            RcDec d;
-            d.init(arc + e.off + 1, e.len - 1);
-            rc_decode_levels(d, band_start, [&](uint32_t p, uint32_t lv) { T[tile_idx(scan[p])] = (int16_t)lv; });
-        }
+        if (tid == 0)
+            rc_decode_levels_lane(arc + e.off + 1, e.len - 1, band_start,
+                                  [&](uint32_t p, uint32_t lv) { T[tile_idx(scan[p])] = (int16_t)lv; });
     } else {
         const uint32_t n = c & kEntMask;
         for (uint32_t i = tid; i < n; i += NT) {

@@ -15,19 +15,25 @@ namespace vcg {
 
 constexpr size_t kTileSmem = 32768 * sizeof(int32_t);
 
-template <int BS>
-__global__ void __launch_bounds__(BS) k_rc_batch(BatchJob J) {
+// Persistent over the batch's distinct atoms (their number is read from device
+// memory): G atoms per warp by rc_lanes_for, scalar decoder for G = 1, lockstep
+// decoder otherwise.
+constexpr int kRcBatchThreads = 128;
+
+__global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
     __shared__ uint32_t bstart[9];
     if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
     __syncthreads();
     const uint32_t n = *J.n_ua;
-    const uint64_t stride = (uint64_t)gridDim.x * BS;
-    // warp-uniform rounds: every lane of a warp takes part in each decode call
-    for (uint64_t base = (uint64_t)blockIdx.x * BS + (threadIdx.x & ~31u); base < n; base += stride) {
-        const uint64_t u = base + (threadIdx.x & 31u);
+    const uint32_t G = rc_lanes_for(n, J.sms, J.rc_scalar_warps);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (G == 1 && lane != 0) return;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (kRcBatchThreads / 32);
+    for (uint64_t w = ((uint64_t)blockIdx.x * kRcBatchThreads + threadIdx.x) >> 5; w * G < n; w += nwarps) {
+        const uint64_t u = w * G + lane;
         bool active = false;
         vcd_atom e = {};
-        if (u < n) {
+        if (lane < G && u < n) {
             e = J.atoms[J.ua[u].idx];
             active = e.kind == VCD_PRESENT;
             if (!active) J.cnt[u] = 0;
@@ -39,11 +45,16 @@ __global__ void __launch_bounds__(BS) k_rc_batch(BatchJob J) {
             if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
             dst = J.ent + J.ent_off[u];
         }
-        int bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart,
-                                        [&](uint32_t p, uint32_t lv) {
-                                            if (cnt < cap) dst[cnt] = p | (lv << 16);
-                                            ++cnt;
-                                        });
+        auto sink = [&](uint32_t p, uint32_t lv) {
+            if (cnt < cap) dst[cnt] = p | (lv << 16);
+            ++cnt;
+        };
+        int bad = 0;
+        if (G == 1) {
+            if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
+        } else {
+            bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart, sink);
+        }
         if (!active) continue;
         J.cnt[u] = (cnt > cap ? cap : cnt) | (cnt > cap ? kEntOverflow : 0u) | (bad ? kEntBad : 0u);
         if (bad) {
@@ -107,13 +118,20 @@ __global__ void __launch_bounds__(NT, 1) k_idct_batch(BatchJob J) {
     }
 }
 
-template <int BS>
 static void launch_rc(const BatchJob &J, int num_sms, uint32_t max_ua, cudaStream_t s) {
-    // enough CTAs for every distinct atom to have its own lane (all resident)
-    uint64_t need = ((uint64_t)max_ua + BS - 1) / BS;
-    uint64_t cap = (uint64_t)num_sms * (2048 / BS);
-    unsigned grid = (unsigned)(need < 1 ? 1 : (need < cap ? need : cap));
-    k_rc_batch<BS><<<grid, BS, 0, s>>>(J);
+    // warps for the widest case up to max_ua atoms: one per atom while the
+    // policy keeps atoms one per warp, else one per 32 atoms; capped at a full
+    // device (the kernel loops)
+    const uint64_t slots = 4ull * (uint64_t)num_sms;
+    const uint64_t scalar = (uint64_t)J.rc_scalar_warps * slots;
+    uint64_t warps = max_ua < scalar ? max_ua : scalar;
+    const uint64_t packed = ((uint64_t)max_ua + 31) / 32;
+    if (packed > warps) warps = packed;
+    const uint64_t cap = (uint64_t)num_sms * (2048 / kRcBatchThreads) * (kRcBatchThreads / 32);
+    if (warps > cap) warps = cap;
+    if (warps < 1) warps = 1;
+    const unsigned grid = (unsigned)((warps * 32 + kRcBatchThreads - 1) / kRcBatchThreads);
+    k_rc_batch<<<grid, kRcBatchThreads, 0, s>>>(J);
 }
 
 template <int NT>
@@ -127,11 +145,10 @@ static void launch_tx(const BatchJob &J, int num_sms, cudaStream_t s) {
 }
 
 void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s) {
-    switch (shape.rc_threads) {
-    case 64: launch_rc<64>(J, num_sms, max_ua, s); break;
-    case 256: launch_rc<256>(J, num_sms, max_ua, s); break;
-    default: launch_rc<128>(J, num_sms, max_ua, s);
-    }
+    BatchJob Jr = J;
+    Jr.rc_scalar_warps = (uint32_t)shape.rc_scalar_warps;
+    Jr.sms = (uint32_t)num_sms;
+    launch_rc(Jr, num_sms, max_ua, s);
     if (shape.idct_threads == 512) launch_tx<512>(J, num_sms, s);
     else launch_tx<256>(J, num_sms, s);
 }

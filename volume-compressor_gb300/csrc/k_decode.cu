@@ -4,7 +4,9 @@
 //   k_caps       one thread per box atom: coefficient-list capacity
 //   k_scan_u64   one CTA: exclusive scan of the capacities (list placement)
 //   k_rc_decode  one thread per PRESENT atom: serial range decode of its
-//                payload into (raster index, level) pairs (src/vc/vc.c:545-560)
+//                payload into (scan position, level) pairs (src/vc/vc.c:545-560);
+//                one atom per warp for small decodes, a warp of atoms in
+//                lockstep for large ones
 //   k_idct       one CTA per atom (persistent over the box): scatter levels into
 //                a 32x32x32 i32 tile in shared memory, dequantise while loading
 //                each z-slab (src/vc/vc.c:327-338), inverse passes along x and y
@@ -86,18 +88,18 @@ __global__ void __launch_bounds__(1024) k_scan_u64(uint64_t *v, uint64_t n, uint
     if (tid == 0 && total) *total = carry_s;
 }
 
-constexpr int kRcThreads = 128;
-
-__global__ void __launch_bounds__(kRcThreads) k_rc_decode(DecodeJob J) {
+// One warp per CTA, G atoms per warp (rc_lanes_for): G = 1 runs the scalar
+// decoder on lane 0, G > 1 the lockstep decoder on lanes 0..G-1.
+__global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G) {
     __shared__ uint32_t bstart[9];
     if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
     __syncthreads();
-    // every lane takes part in the warp-lockstep decoder; lanes without a
-    // PRESENT atom run along inactive
-    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x;
+    if (G == 1 && lane != 0) return;
+    const uint64_t t = (uint64_t)blockIdx.x * G + lane;
     bool active = false;
     vcd_atom e = {};
-    if (t < J.n_atoms) {
+    if (lane < G && t < J.n_atoms) {
         uint32_t az, ay, ax;
         box_atom(J, t, az, ay, ax);
         e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
@@ -112,16 +114,26 @@ __global__ void __launch_bounds__(kRcThreads) k_rc_decode(DecodeJob J) {
         dst = J.ent + J.ent_off[t];
     }
     // entries carry the scan position; the transform kernel maps it to raster
-    int bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart,
-                                    [&](uint32_t p, uint32_t lv) {
-                                        if (n < cap) dst[n] = p | (lv << 16);
-                                        ++n;
-                                    });
+    auto sink = [&](uint32_t p, uint32_t lv) {
+        if (n < cap) dst[n] = p | (lv << 16);
+        ++n;
+    };
+    int bad = 0;
+    if (G == 1) {
+        if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
+    } else {
+        bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart, sink);
+    }
     if (!active) return;
     uint32_t flags = (n > cap ? kEntOverflow : 0u) | (bad ? kEntBad : 0u);
     J.cnt[t] = (n > cap ? cap : n) | flags;
     atomicAdd(J.nnz_total, (unsigned long long)(n > cap ? cap : n));
     if (bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
+}
+
+static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s) {
+    const uint32_t G = rc_lanes_for(J.n_atoms, (uint32_t)num_sms, rc_scalar_warps());
+    k_rc_decode<<<(unsigned)((J.n_atoms + G - 1) / G), 32, 0, s>>>(J, G);
 }
 
 __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
@@ -168,8 +180,7 @@ void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s) {
         attr = true;
     }
     if (!J.n_atoms) return;
-    unsigned nb = (unsigned)((J.n_atoms + 127) / 128);
-    k_rc_decode<<<nb, 128, 0, s>>>(J);
+    launch_rc(J, num_sms, s);
     uint64_t grid = J.n_atoms < (uint64_t)num_sms ? J.n_atoms : (uint64_t)num_sms;
     k_idct<<<(unsigned)grid, kIdctThreads, kIdctSmem, s>>>(J);
 }
@@ -187,7 +198,7 @@ void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageE
         launch_scan_u64(J.ent_off, J.n_atoms, 0, nullptr, s);
     }
     if (ev) cudaEventRecord(ev->ev[1], s);
-    if (J.n_atoms) k_rc_decode<<<nb, 128, 0, s>>>(J);
+    if (J.n_atoms) launch_rc(J, num_sms, s);
     if (ev) cudaEventRecord(ev->ev[2], s);
     if (J.n_atoms) {
         uint64_t grid = J.n_atoms < (uint64_t)num_sms ? J.n_atoms : (uint64_t)num_sms;

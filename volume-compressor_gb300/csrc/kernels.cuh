@@ -65,11 +65,30 @@ struct BatchJob {
     uint32_t *work;              // transform work counter (reset per batch)
     uint32_t *req_err;           // per request: set when one of its atoms is malformed
     uint32_t band_start[9];
+    uint32_t sms;                // SM count of the device
+    uint32_t rc_scalar_warps;    // range-decoder policy (rc_lanes_for)
 };
 struct BatchShape {              // tunables the autotuner chooses among
-    int rc_threads;              // range-decoder CTA size: 64, 128, 256
+    int rc_scalar_warps;         // range-decoder policy: 1, 4 or 16 (rc_lanes_for)
     int idct_threads;            // transform CTA size (warps per atom x 32): 256 or 512
 };
+
+// Atoms per warp for the range decoder. A warp that decodes one atom runs the
+// scalar decoder, whose latency per atom is the lowest; a warp of several atoms
+// runs them in lockstep, which costs more decision steps per atom but issues
+// each instruction for all of them. One atom per warp while that makes at most
+// `scalar_warps` warps per SM sub-partition (4 per SM), else the smallest power
+// of two that keeps to about one warp per sub-partition, at most 32.
+__host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms, uint32_t scalar_warps) {
+    const uint64_t slots = 4ull * sms;
+    if (n_atoms <= (uint64_t)scalar_warps * slots) return 1;
+    uint32_t g = 2;
+    while (g < 32 && (uint64_t)g * slots < n_atoms) g <<= 1;
+    return g;
+}
+constexpr uint32_t kRcScalarWarpsDefault = 4;
+// policy of the plain decode path (vcg_set_rc_scalar_warps)
+uint32_t rc_scalar_warps();
 void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s);
 
 void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev);

@@ -1,8 +1,9 @@
 // Batched region decode orchestration: upload the batch description (distinct
 // atoms, their destination lists, the request boxes, list offsets) into
 // grow-only device buffers, then replay one CUDA graph of the persistent
-// range-decode + transform launches. The launch shape (range-decoder CTA size,
-// transform CTA size) is picked once per process by timing every candidate on
+// range-decode + transform launches. The launch shape (range-decoder policy:
+// warps per SM sub-partition that decode one atom each before atoms share warps
+// in lockstep; transform CTA size = 32 x warps per atom) is picked once per process by timing every candidate on
 // the first batch (all candidates produce identical bytes); threads that start
 // later take the tuned shape.
 #include <cuda_runtime.h>
@@ -18,7 +19,7 @@ using namespace vcg;
 
 #define VC_API extern "C" __attribute__((visibility("default")))
 
-static const BatchShape kShapes[] = {{64, 256}, {128, 256}, {256, 256}, {64, 512}, {128, 512}, {256, 512}};
+static const BatchShape kShapes[] = {{1, 256}, {4, 256}, {16, 256}, {1, 512}, {4, 512}, {16, 512}};
 
 #define CKB(call, what)                                \
     do {                                               \
@@ -89,11 +90,11 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
     // capacity in distinct atoms the range-decode grid must cover (the buffer's)
     const uint32_t max_ua = (uint32_t)((cap_of(c, VCD_BUF_BUA) - 64) / sizeof(vcd_uatom));
 
-    if (!c->batch_rc_threads) {
+    if (!c->batch_rc_scalar_warps) {
         const int t = __atomic_load_n(&g_tuned_shape, __ATOMIC_ACQUIRE);
-        if (t) { c->batch_rc_threads = t >> 16; c->batch_tx_threads = t & 0xFFFF; }
+        if (t) { c->batch_rc_scalar_warps = t >> 16; c->batch_tx_threads = t & 0xFFFF; }
     }
-    if (!c->batch_rc_threads) {   // autotune on the process's first batch
+    if (!c->batch_rc_scalar_warps) {   // autotune on the process's first batch
         float best = 1e30f;
         for (const BatchShape &s : kShapes) {
             CKB(cudaMemsetAsync(ctl + 1, 0, 4, st), "reset");
@@ -103,13 +104,13 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
             CKB(cudaEventSynchronize(c->ev[1]), "autotune");
             CKB(cudaGetLastError(), "autotune");
             float ms = vcd_elapsed(c->ev[0], c->ev[1]);
-            if (ms < best) { best = ms; c->batch_rc_threads = s.rc_threads; c->batch_tx_threads = s.idct_threads; }
+            if (ms < best) { best = ms; c->batch_rc_scalar_warps = s.rc_scalar_warps; c->batch_tx_threads = s.idct_threads; }
         }
         CKB(cudaMemsetAsync(ctl + 1, 0, 4, st), "reset");
         CKB(cudaMemsetAsync(ctl + 4, 0, (size_t)b->n_req * 4, st), "reset");
-        __atomic_store_n(&g_tuned_shape, c->batch_rc_threads << 16 | c->batch_tx_threads, __ATOMIC_RELEASE);
+        __atomic_store_n(&g_tuned_shape, c->batch_rc_scalar_warps << 16 | c->batch_tx_threads, __ATOMIC_RELEASE);
     }
-    const BatchShape shape = {c->batch_rc_threads, c->batch_tx_threads};
+    const BatchShape shape = {c->batch_rc_scalar_warps, c->batch_tx_threads};
     // the graph bakes in every kernel parameter (buffers, archive tables) and the
     // grid size: replay it only when all of them are unchanged
     unsigned char key[512];
@@ -162,8 +163,8 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
 }
 
 // Launch shape the calling thread uses (0 before its first batch).
-VC_API void vcg_batch_shape(int *rc_threads, int *transform_threads) {
+VC_API void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads) {
     vcd_ctx *c = vcd_thread_ctx();
-    if (rc_threads) *rc_threads = c ? c->batch_rc_threads : 0;
+    if (rc_scalar_warps) *rc_scalar_warps = c ? c->batch_rc_scalar_warps : 0;
     if (transform_threads) *transform_threads = c ? c->batch_tx_threads : 0;
 }

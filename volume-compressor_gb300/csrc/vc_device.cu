@@ -143,6 +143,14 @@ extern "C" __attribute__((visibility("default"))) double vcg_last_call_ms(void) 
     return c ? c->last_ms : -1.0;
 }
 
+// Range-decoder policy of the plain decode path (rc_lanes_for).
+static uint32_t g_rc_scalar_warps = vcg::kRcScalarWarpsDefault;
+uint32_t vcg::rc_scalar_warps() { return __atomic_load_n(&g_rc_scalar_warps, __ATOMIC_RELAXED); }
+extern "C" __attribute__((visibility("default"))) void vcg_set_rc_scalar_warps(int w) {
+    const uint32_t v = w <= 0 ? vcg::kRcScalarWarpsDefault : (uint32_t)(w > 64 ? 64 : w);
+    __atomic_store_n(&g_rc_scalar_warps, v, __ATOMIC_RELAXED);
+}
+
 // grow-only scratch buffer `slot` of the calling thread
 cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out) {
     if (bytes == 0) bytes = 16;
