@@ -45,6 +45,9 @@ def args_parse():
     p.add_argument("--regions", type=int, default=200)
     p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched-region measurement")
     p.add_argument("--no-served", action="store_true", help="skip the config-5 served-decode measurement")
+    p.add_argument("--no-dct", action="store_true", help="skip the config-3 DCT-forms measurement")
+    p.add_argument("--dct-size", type=int, default=1024, help="edge of the DCT-forms volume")
+    p.add_argument("--dct-reps", type=int, default=3, help="timed calls per DCT form and direction (0: one call)")
     return p.parse_args()
 
 
@@ -280,6 +283,97 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             "speedup_vs_plain": batch_gbps / plain_gbps, "autotuned_shape": {"rc_scalar_warps": shape[0],
                                                                             "transform_threads": shape[1]},
             "bit_exact_sample": ok, "plain_sample": plain_sample}
+
+
+def _equal_device(vc, a, b, nbytes, chunk=256 << 20):
+    """Byte-compare two device buffers chunk by chunk on the host."""
+    import numpy as np
+    ha = np.empty(min(chunk, nbytes), np.uint8)
+    hb = np.empty(min(chunk, nbytes), np.uint8)
+    L = vc.lib()
+    for o in range(0, nbytes, chunk):
+        n = min(chunk, nbytes - o)
+        L.vcg_copy(ha.ctypes.data, ctypes.c_void_p(a.ptr + o), n)
+        L.vcg_copy(hb.ctypes.data, ctypes.c_void_p(b.ptr + o), n)
+        if not np.array_equal(ha[:n], hb[:n]):
+            return False
+    return True
+
+
+def config3_dct(n=1024, centre=128, reps=3, sample_atoms=256):
+    """Whole-atom integer DCT of the 1024^3 volume (u8 centred by 128), forward
+    and inverse, in both forms: butterfly (CUDA cores) and IMMA (int8 tensor
+    cores, hi/lo pieces). Every coefficient and voxel of the two forms is
+    compared; the CPU leg times the C restatement of the reference transform
+    on a bounded sample of atoms and checks the device outputs of those atoms."""
+    import numpy as np
+    import vc_gb300 as vc
+    dims = (n, n, n)
+    vol = vc.synth_device(n, n, n, vc.config_seed(3))
+    coef = [vc.DeviceBuffer(n ** 3 * 4) for _ in range(2)]
+    rec = [vc.DeviceBuffer(n ** 3) for _ in range(2)]
+    res = {}
+    for form, name in ((vc.DCT_BUTTERFLY, "butterfly"), (vc.DCT_IMMA, "imma")):
+        fwd, inv = [], []
+        for r in range(reps + 1):
+            s, redone = vc.dct_forward(vol, dims, centre, form, coef[form])
+            assert s == 0 and redone == 0, vc.last_error()
+            if r or not reps:
+                fwd.append(vc.last_call_ms())
+        for r in range(reps + 1):
+            s, redone = vc.dct_inverse(coef[form], dims, centre, form, rec[form])
+            assert s == 0, vc.last_error()
+            if r or not reps:
+                inv.append(vc.last_call_ms())
+        f, i = min(fwd), min(inv)
+        res[name] = {"forward_ms": f, "inverse_ms": i, "inverse_atoms_redone": redone,
+                     "forward_voxel_GBps": n ** 3 / (f / 1e3) / 1e9,
+                     "forward_hbm_GBps": 5 * n ** 3 / (f / 1e3) / 1e9,
+                     "inverse_voxel_GBps": n ** 3 / (i / 1e3) / 1e9,
+                     "inverse_hbm_GBps": 5 * n ** 3 / (i / 1e3) / 1e9}
+    forms_equal = _equal_device(vc, coef[0], coef[1], n ** 3 * 4) and _equal_device(vc, rec[0], rec[1], n ** 3)
+    # CPU leg: the C restatement of the reference transform on a bounded sample of atoms
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oraclelib
+    O = oraclelib.lib()
+    rng = np.random.default_rng(0xD7C3)
+    na = n // 32
+    picks = rng.choice(na ** 3, min(sample_atoms, na ** 3), replace=False)
+    host_vol = np.empty((32, 32, 32), np.uint8)
+    ok = True
+    t_cpu = 0.0
+    L = vc.lib()
+    for a in picks:
+        a = int(a)
+        ax, ay, az = a % na, (a // na) % na, a // (na * na)
+        for z in range(32):
+            for y in range(32):
+                L.vcg_copy(host_vol[z, y].ctypes.data,
+                           ctypes.c_void_p(vol.ptr + ((az * 32 + z) * n + ay * 32 + y) * n + ax * 32), 32)
+        c_ref = np.empty(32768, np.int32)
+        v_ref = np.empty(32768, np.uint8)
+        t0 = time.perf_counter()
+        O.orc_fdct(host_vol.ctypes.data, centre, c_ref.ctypes.data)
+        O.orc_idct(c_ref.ctypes.data, centre, v_ref.ctypes.data)
+        t_cpu += time.perf_counter() - t0
+        c_dev = np.empty(32768, np.int32)
+        L.vcg_copy(c_dev.ctypes.data, ctypes.c_void_p(coef[1].ptr + a * 32768 * 4), 32768 * 4)
+        v_dev = np.empty((32, 32, 32), np.uint8)
+        for z in range(32):
+            for y in range(32):
+                L.vcg_copy(v_dev[z, y].ctypes.data,
+                           ctypes.c_void_p(rec[1].ptr + ((az * 32 + z) * n + ay * 32 + y) * n + ax * 32), 32)
+        ok = ok and bool(np.array_equal(c_dev, c_ref)) and bool(np.array_equal(v_dev.ravel(), v_ref))
+    for b in coef + rec + [vol]:
+        b.free()
+    return {"workload": f"{n}^3 u8 synthetic volume (seed 0x5EED0003), {na ** 3} atoms, centre {centre}, "
+                        "forward + inverse 3-D DCT-32",
+            **res, "imma_vs_butterfly_forward_speedup": res["butterfly"]["forward_ms"] / res["imma"]["forward_ms"],
+            "imma_vs_butterfly_inverse_speedup": res["butterfly"]["inverse_ms"] / res["imma"]["inverse_ms"],
+            "forms_identical_all_outputs": forms_equal,
+            "cpu_reference": {"atoms": sample_atoms, "threads": 1, "kind": "port",
+                              "voxel_MBps_forward_plus_inverse": sample_atoms * 32768 / t_cpu / 1e6,
+                              "bit_exact_sample": ok}}
 
 
 def served_mix(a, rng, n):
@@ -589,19 +683,19 @@ def gb300_arm(args, dist):
         if lod0_ok is None:
             lod0_ok = bool(np.array_equal(out.download(nbytes), ref_out.ravel()))
 
-    batched = None
-    if dist.rank == 0 and not args.no_batched:
+    # the other workloads (rank 0): release the headline buffers first
+    batched = dct = served = None
+    if dist.rank == 0 and not (args.no_batched and args.no_dct and args.no_served):
         arc.close()
         out.free()
         flush.free()
-        batched = config4_batched()
-    served = None
-    if dist.rank == 0 and not args.no_served:
-        if args.no_batched:
-            arc.close()
-            out.free()
-            flush.free()
-        served = config5_served()
+        dvol.free()
+        if not args.no_batched:
+            batched = config4_batched()
+        if not args.no_dct:
+            dct = config3_dct(n=args.dct_size, reps=args.dct_reps)
+        if not args.no_served:
+            served = config5_served()
     if dist.rank != 0:
         return
     line = {
@@ -634,6 +728,8 @@ def gb300_arm(args, dist):
         line["batched_regions"] = batched
     if served:
         line["served_regions"] = served
+    if dct:
+        line["dct_forms"] = dct
     print(json.dumps(line), flush=True)
 
 

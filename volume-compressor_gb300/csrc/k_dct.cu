@@ -1,0 +1,397 @@
+// Exact integer 3-D DCT-32 of whole atoms, in two forms (device + C ABI).
+//
+// The transform is the reference's (src/vc/vc.c:77-229): voxels minus a centre
+// value, then along x, y and z the Q14 matrix CMATA with (acc + 2^13) >> 14
+// after every pass and i32 sums with wrap-around; the inverse applies CMATA^T
+// along x, y and z in the same way and adds the centre back, clamped to
+// [0, 255]. Coefficients of an atom are 32768 i32 in (kz, ky, kx) raster order.
+//
+//   butterfly  CUDA cores: one CTA per atom, the recursive even/odd partial
+//              butterfly of dct32.cuh per line (344 multiplies per line).
+//   imma       int8 tensor cores (mma.sync m16n8k32, s8 x s8 -> s32): every
+//              pass is OUT = C V over the atom's 1024 lines, 8 lines per MMA
+//              tile. CMATA entries (|c| <= 4091) are split into two int8 pieces
+//              c = 128 c1 + c0 (c0 = c & 127, c1 = c >> 7) and every pass input
+//              into VP pieces v = sum_j 128^j v_j (v_j = (v >> 7j) & 127 below
+//              the top piece, the top piece v >> 7(VP-1), signed). Products of
+//              equal weight 128^(cp+j) share an s32 accumulator; the
+//              accumulators are recombined by shift-add modulo 2^32, which is
+//              the reference's i32 sum, so the rounded outputs are the same
+//              bits. Intermediates stay in shared memory as int8 piece planes.
+//              Forward inputs provably fit two pieces (|vox - centre| <= 255,
+//              after one pass <= 2038, after two <= 16285 < 2^14); inverse
+//              inputs take three (|v| < 2^21), and an atom whose values leave
+//              that range in any pass is redone with the butterfly, so every
+//              input gives the reference's result.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/vcg.h"
+#include "dct32.cuh"
+#include "vc_device.h"
+
+namespace vcg {
+
+struct DctJob {
+    const uint8_t *vol_in;     // forward input volume
+    const int32_t *coef_in;    // inverse input coefficients
+    int32_t *coef_out;         // forward output coefficients
+    uint8_t *vol_out;          // inverse output volume
+    uint64_t nx, ny, nz;       // volume dims (multiples of 32)
+    uint32_t ax, ay;           // atoms along x and y
+    uint64_t n_atoms;
+    int32_t centre;
+    uint32_t *redone;          // atoms the imma form redid with the butterfly
+};
+
+constexpr int kDctThreads = 256;
+constexpr size_t kTileBytes = 32768 * sizeof(int32_t);
+
+__device__ __forceinline__ void atom_xyz(const DctJob &J, uint64_t a, uint64_t &bx, uint64_t &by, uint64_t &bz) {
+    bx = (a % J.ax) * 32;
+    by = ((a / J.ax) % J.ay) * 32;
+    bz = (a / ((uint64_t)J.ax * J.ay)) * 32;
+}
+
+__device__ __forceinline__ uint8_t clamp_u8(int32_t v) { return (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v)); }
+
+// ------------------------------------------------------------------ butterfly
+// One atom through the three passes with T as a 32 slabs x swizzled 32x32 i32
+// tile (element (z, y, x) at z*1024 + swz(y, x)): x and y per slab (warp per
+// slab, lane per line), then z per column (thread per column) straight to the
+// output. Starts and ends with the CTA converged.
+template <bool INV>
+__device__ void bf_atom(int32_t *T, const DctJob &J, uint64_t a) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint64_t bx, by, bz;
+    atom_xyz(J, a, bx, by, bz);
+    if (!INV) {
+        for (int i = tid; i < 2048; i += kDctThreads) {   // 16 voxels of row (z, y)
+            const int row = i >> 1, x0 = (i & 1) * 16, z = row >> 5, y = row & 31;
+            const uint4 w = *reinterpret_cast<const uint4 *>(J.vol_in + ((bz + z) * J.ny + by + y) * J.nx + bx + x0);
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int b = 0; b < 16; ++b)
+                T[z * 1024 + swz(y, x0 + b)] = (int32_t)((ws[b >> 2] >> (8 * (b & 3))) & 0xFFu) - J.centre;
+        }
+    } else {
+        const int4 *src = reinterpret_cast<const int4 *>(J.coef_in + a * 32768);
+        for (int i = tid; i < 8192; i += kDctThreads) {
+            const int4 w = src[i];
+            const int z = i >> 8, y = (i >> 3) & 31, x = (i & 7) * 4;
+            T[z * 1024 + swz(y, x)] = w.x;
+            T[z * 1024 + swz(y, x + 1)] = w.y;
+            T[z * 1024 + swz(y, x + 2)] = w.z;
+            T[z * 1024 + swz(y, x + 3)] = w.w;
+        }
+    }
+    __syncthreads();
+    for (int z = warp; z < 32; z += kDctThreads / 32) {
+        int32_t *S = T + z * 1024;
+        int32_t v[32], o[32];
+#pragma unroll
+        for (int x = 0; x < 32; ++x) v[x] = S[swz(lane, x)];
+        if (INV) idct32_line(v, o); else fdct32_line(v, o);
+#pragma unroll
+        for (int x = 0; x < 32; ++x) S[swz(lane, x)] = o[x];
+        __syncwarp();
+#pragma unroll
+        for (int y = 0; y < 32; ++y) v[y] = S[swz(y, lane)];
+        if (INV) idct32_line(v, o); else fdct32_line(v, o);
+#pragma unroll
+        for (int y = 0; y < 32; ++y) S[swz(y, lane)] = o[y];
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int c = tid; c < 1024; c += kDctThreads) {
+        const int y = c >> 5, x = c & 31;
+        int32_t v[32], o[32];
+#pragma unroll
+        for (int z = 0; z < 32; ++z) v[z] = T[z * 1024 + swz(y, x)];
+        if (INV) {
+            idct32_line(v, o);
+#pragma unroll
+            for (int z = 0; z < 32; ++z)
+                J.vol_out[((bz + z) * J.ny + by + y) * J.nx + bx + x] = clamp_u8(o[z] + J.centre);
+        } else {
+            fdct32_line(v, o);
+            int32_t *dst = J.coef_out + a * 32768 + y * 32 + x;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) dst[k * 1024] = o[k];
+        }
+    }
+    __syncthreads();
+}
+
+template <bool INV>
+__global__ void __launch_bounds__(kDctThreads, 1) k_dct_bf(DctJob J) {
+    extern __shared__ __align__(16) int32_t T[];
+    for (uint64_t a = blockIdx.x; a < J.n_atoms; a += gridDim.x) bf_atom<INV>(T, J, a);
+}
+
+// ------------------------------------------------------------------ imma
+__constant__ int32_t c_cmat[32][32] = VC_CMAT_INIT;
+
+// Byte of element n in a 32-byte piece line, arranged so that lane (g, t) of
+// an m16n8k32 B fragment finds its elements n = 4t..4t+3 and 16+4t..16+4t+3 as
+// one aligned 8-byte word.
+__device__ __forceinline__ int ppos(int n) { return (((n & 15) >> 2) << 3) | ((n >> 4) << 2) | (n & 3); }
+
+__device__ __forceinline__ void mma_s8(int32_t (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+r"(d[0]), "+r"(d[1]), "+r"(d[2]), "+r"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// piece j of v (VP pieces): low pieces 7 bits, the top piece signed
+template <int VP>
+__device__ __forceinline__ uint32_t piece(int32_t v, int j) {
+    return j < VP - 1 ? (uint32_t)(v >> (7 * j)) & 127u : (uint32_t)(v >> (7 * (VP - 1))) & 0xFFu;
+}
+template <int VP>
+__device__ __forceinline__ bool fits(int32_t v) {
+    const int32_t top = v >> (7 * (VP - 1));
+    return top >= -128 && top <= 127;
+}
+
+template <bool INV, int VP>
+__global__ void __launch_bounds__(kDctThreads, 1) k_dct_imma(DctJob J) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    __shared__ int s_bad;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g = lane >> 2, t = lane & 3;
+    // A fragments of the two coefficient pieces: rows g, g+8 (+16 per m-tile),
+    // columns 4t..4t+3 and 16+4t..16+4t+3; A = C (forward) or C^T (inverse)
+    uint32_t A[2][2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int cp = 0; cp < 2; ++cp)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int row = mt * 16 + g + (r & 1) * 8, col0 = (r >> 1) * 16 + t * 4;
+                uint32_t w = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const int32_t c = INV ? c_cmat[col0 + b][row] : c_cmat[row][col0 + b];
+                    const uint32_t p = cp ? (uint32_t)(c >> 7) & 0xFFu : (uint32_t)c & 127u;
+                    w |= p << (8 * b);
+                }
+                A[mt][cp][r] = w;
+            }
+    // piece plane j of ping-pong buffer b
+    auto plane = [&](int b, int j) -> uint8_t * { return sm + (b * VP + j) * 32768; };
+
+    for (uint64_t a = blockIdx.x; a < J.n_atoms; a += gridDim.x) {
+        uint64_t bx, by, bz;
+        atom_xyz(J, a, bx, by, bz);
+        if (tid == 0) s_bad = 0;
+        bool bad = false;
+        // pass-0 input: line (z, y), element x
+        if (!INV) {
+            for (int i = tid; i < 2048; i += kDctThreads) {
+                const int row = i >> 1, half = i & 1, z = row >> 5, y = row & 31;
+                const uint4 w = *reinterpret_cast<const uint4 *>(J.vol_in + ((bz + z) * J.ny + by + y) * J.nx + bx +
+                                                                 half * 16);
+                const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t pk[VP];
+#pragma unroll
+                    for (int j = 0; j < VP; ++j) pk[j] = 0;
+#pragma unroll
+                    for (int i4 = 0; i4 < 4; ++i4) {
+                        const int32_t v = (int32_t)((ws[q] >> (8 * i4)) & 0xFFu) - J.centre;
+#pragma unroll
+                        for (int j = 0; j < VP; ++j) pk[j] |= piece<VP>(v, j) << (8 * i4);
+                    }
+#pragma unroll
+                    for (int j = 0; j < VP; ++j)
+                        *reinterpret_cast<uint32_t *>(plane(0, j) + row * 32 + q * 8 + half * 4) = pk[j];
+                }
+            }
+        } else {
+            const int4 *src = reinterpret_cast<const int4 *>(J.coef_in + a * 32768);
+            for (int i = tid; i < 8192; i += kDctThreads) {
+                const int4 w = src[i];
+                const int row = i >> 3, n0 = (i & 7) * 4;
+                const int32_t vs[4] = {w.x, w.y, w.z, w.w};
+                uint32_t pk[VP];
+#pragma unroll
+                for (int j = 0; j < VP; ++j) pk[j] = 0;
+#pragma unroll
+                for (int i4 = 0; i4 < 4; ++i4) {
+                    bad |= !fits<VP>(vs[i4]);
+#pragma unroll
+                    for (int j = 0; j < VP; ++j) pk[j] |= piece<VP>(vs[i4], j) << (8 * i4);
+                }
+#pragma unroll
+                for (int j = 0; j < VP; ++j) *reinterpret_cast<uint32_t *>(plane(0, j) + row * 32 + ppos(n0)) = pk[j];
+            }
+        }
+        __syncthreads();
+
+#pragma unroll 1
+        for (int pass = 0; pass < 3; ++pass) {
+            const int sb = pass & 1, db = sb ^ 1;
+#pragma unroll 1
+            for (int tile = warp; tile < 128; tile += kDctThreads / 32) {
+                const int L0 = tile * 8;
+                uint32_t B[VP][2];
+#pragma unroll
+                for (int j = 0; j < VP; ++j) {
+                    const uint2 w = *reinterpret_cast<const uint2 *>(plane(sb, j) + (L0 + g) * 32 + t * 8);
+                    B[j][0] = w.x;
+                    B[j][1] = w.y;
+                }
+                int32_t acc[2][VP + 1][4];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int w = 0; w <= VP; ++w)
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) acc[mt][w][r] = 0;
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int cp = 0; cp < 2; ++cp)
+#pragma unroll
+                        for (int j = 0; j < VP; ++j) mma_s8(acc[mt][cp + j], A[mt][cp], B[j][0], B[j][1]);
+                // epilogue: lane holds rows k = 16 mt + 8 h + g of lines L0 + 2t, L0 + 2t + 1
+                const int line = L0 + 2 * t, la = line >> 5, lb = line & 31;
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = mt * 16 + h * 8 + g;
+                        int32_t o[2];
+#pragma unroll
+                        for (int e = 0; e < 2; ++e) {
+                            uint32_t s = 0;
+#pragma unroll
+                            for (int w = 0; w <= VP; ++w) s += (uint32_t)acc[mt][w][h * 2 + e] << (7 * w);
+                            o[e] = (int32_t)(s + 8192u) >> 14;
+                        }
+                        if (pass < 2) {
+                            // rotate (a, b, k) -> line' = k*32 + a, element b
+                            bad |= !fits<VP>(o[0]) || !fits<VP>(o[1]);
+                            const int off = (k * 32 + la) * 32 + ppos(lb);
+#pragma unroll
+                            for (int j = 0; j < VP; ++j)
+                                *reinterpret_cast<uint16_t *>(plane(db, j) + off) =
+                                    (uint16_t)(piece<VP>(o[0], j) | (piece<VP>(o[1], j) << 8));
+                        } else if (!INV) {
+                            *reinterpret_cast<int2 *>(J.coef_out + a * 32768 + (k * 32 + la) * 32 + lb) =
+                                make_int2(o[0], o[1]);
+                        } else {
+                            const uint32_t v2 = (uint32_t)clamp_u8(o[0] + J.centre) |
+                                                ((uint32_t)clamp_u8(o[1] + J.centre) << 8);
+                            *reinterpret_cast<uint16_t *>(J.vol_out + ((bz + k) * J.ny + by + la) * J.nx + bx + lb) =
+                                (uint16_t)v2;
+                        }
+                    }
+            }
+            if (bad) s_bad = 1;
+            __syncthreads();
+        }
+        if (s_bad) {   // a value left the piece range: redo the atom exactly
+            if (tid == 0) atomicAdd(J.redone, 1u);
+            bf_atom<INV>(reinterpret_cast<int32_t *>(sm), J, a);
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace vcg
+
+using namespace vcg;
+
+#define VC_API extern "C" __attribute__((visibility("default")))
+
+static vc_status dct_run(const void *in, void *out, vc_dims dims, int centre, int form, int inverse,
+                         uint32_t *redone) {
+    if (!in || !out || !dims.nx || !dims.ny || !dims.nz || (dims.nx | dims.ny | dims.nz) & 31u ||
+        dims.nx > VC_MAX_DIM || dims.ny > VC_MAX_DIM || dims.nz > VC_MAX_DIM || centre < 0 || centre > 255 ||
+        (form != VCG_DCT_BUTTERFLY && form != VCG_DCT_IMMA) || ((uintptr_t)in & 15u) || ((uintptr_t)out & 15u))
+        return VC_ERR_RANGE;
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return VC_ERR_IO;
+    cudaPointerAttributes pa, pb;
+    if (cudaPointerGetAttributes(&pa, in) != cudaSuccess || cudaPointerGetAttributes(&pb, out) != cudaSuccess ||
+        pa.type != cudaMemoryTypeDevice || pb.type != cudaMemoryTypeDevice) {
+        cudaGetLastError();
+        return VC_ERR_RANGE;
+    }
+    void *p_red;
+    cudaError_t e = vcd_scratch(c, VCD_BUF_RED, 64, &p_red);
+    if (e != cudaSuccess) {
+        vcd_set_error("dct scratch", e);
+        return (vc_status)vcd_status_of(e);
+    }
+    DctJob J;
+    memset(&J, 0, sizeof J);
+    J.vol_in = inverse ? nullptr : (const uint8_t *)in;
+    J.coef_in = inverse ? (const int32_t *)in : nullptr;
+    J.coef_out = inverse ? nullptr : (int32_t *)out;
+    J.vol_out = inverse ? (uint8_t *)out : nullptr;
+    J.nx = dims.nx;
+    J.ny = dims.ny;
+    J.nz = dims.nz;
+    J.ax = dims.nx / 32;
+    J.ay = dims.ny / 32;
+    J.n_atoms = (uint64_t)J.ax * J.ay * (dims.nz / 32);
+    J.centre = centre;
+    J.redone = (uint32_t *)p_red;
+    const unsigned grid = (unsigned)(J.n_atoms < (uint64_t)g_dev.num_sms ? J.n_atoms : (uint64_t)g_dev.num_sms);
+    cudaStream_t st = c->stream;
+    cudaMemsetAsync(p_red, 0, 4, st);
+    cudaEventRecord(c->ev[0], st);
+    const char *name;
+    if (form == VCG_DCT_BUTTERFLY) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_dct_bf<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileBytes);
+            cudaFuncSetAttribute(k_dct_bf<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileBytes);
+            attr = true;
+        }
+        if (inverse) k_dct_bf<true><<<grid, kDctThreads, kTileBytes, st>>>(J);
+        else k_dct_bf<false><<<grid, kDctThreads, kTileBytes, st>>>(J);
+        name = inverse ? "dct_inverse_butterfly" : "dct_forward_butterfly";
+    } else {
+        static bool attr = false;
+        const size_t fwd_smem = 2 * 2 * 32768, inv_smem = 2 * 3 * 32768;
+        if (!attr) {
+            cudaFuncSetAttribute(k_dct_imma<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem);
+            cudaFuncSetAttribute(k_dct_imma<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)inv_smem);
+            attr = true;
+        }
+        if (inverse) k_dct_imma<true, 3><<<grid, kDctThreads, inv_smem, st>>>(J);
+        else k_dct_imma<false, 2><<<grid, kDctThreads, fwd_smem, st>>>(J);
+        name = inverse ? "dct_inverse_imma" : "dct_forward_imma";
+    }
+    cudaEventRecord(c->ev[1], st);
+    uint32_t red = 0;
+    cudaMemcpyAsync(&red, p_red, 4, cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) {
+        vcd_set_error("dct kernels", e);
+        return (vc_status)vcd_status_of(e);
+    }
+    c->last_ms = vcd_elapsed(c->ev[0], c->ev[1]);
+    if (redone) *redone = red;
+    if (vcd_prof_on()) {
+        const uint64_t vox = J.n_atoms * 32768ull;
+        vcd_prof_add(name, c->last_ms, 1, inverse ? 4 * vox : vox, inverse ? vox : 4 * vox, J.n_atoms);
+    }
+    return VC_OK;
+}
+
+VC_API vc_status vcg_dct_forward(const uint8_t *vol_dev, vc_dims dims, int centre, int form, int32_t *coef_dev,
+                                 uint32_t *redone) {
+    return dct_run(vol_dev, coef_dev, dims, centre, form, 0, redone);
+}
+
+VC_API vc_status vcg_dct_inverse(const int32_t *coef_dev, vc_dims dims, int centre, int form, uint8_t *vol_dev,
+                                 uint32_t *redone) {
+    return dct_run(coef_dev, vol_dev, dims, centre, form, 1, redone);
+}

@@ -22,7 +22,7 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
               "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_rc_scalar_warps",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_rc_scalar_warps", "vcg_dct_forward", "vcg_dct_inverse",
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
@@ -82,6 +82,23 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+DCT_BUTTERFLY, DCT_IMMA = 0, 1
+
+
+def dct_forward(vol, dims, centre, form, coef):
+    """vcg_dct_forward: vol, coef DeviceBuffers; dims (nx, ny, nz). Returns (status, atoms redone)."""
+    r = ctypes.c_uint32()
+    s = lib().vcg_dct_forward(vol.ptr, Dims(*dims), centre, form, coef.ptr, ctypes.byref(r))
+    return s, r.value
+
+
+def dct_inverse(coef, dims, centre, form, vol):
+    """vcg_dct_inverse: coef, vol DeviceBuffers; dims (nx, ny, nz). Returns (status, atoms redone)."""
+    r = ctypes.c_uint32()
+    s = lib().vcg_dct_inverse(coef.ptr, Dims(*dims), centre, form, vol.ptr, ctypes.byref(r))
+    return s, r.value
 
 
 def batch_shape():
@@ -146,6 +163,8 @@ def lib():
         L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
         L.vcg_batch_shape.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.vcg_set_rc_scalar_warps.argtypes = [ctypes.c_int]
+        L.vcg_dct_forward.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
+        L.vcg_dct_inverse.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
         L.vcg_server_create.restype = P
         L.vcg_server_create.argtypes = [P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int]
         L.vcg_server_submit.restype = ctypes.c_int64
