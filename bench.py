@@ -300,28 +300,31 @@ def _equal_device(vc, a, b, nbytes, chunk=256 << 20):
     return True
 
 
-def config3_dct(n=1024, centre=128, reps=3, sample_atoms=256):
-    """Whole-atom integer DCT of the 1024^3 volume (u8 centred by 128), forward
-    and inverse, in both forms: butterfly (CUDA cores) and IMMA (int8 tensor
-    cores, hi/lo pieces). Every coefficient and voxel of the two forms is
-    compared; the CPU leg times the C restatement of the reference transform
-    on a bounded sample of atoms and checks the device outputs of those atoms."""
+def config3_dct(n=1024, reps=3, sample_atoms=256):
+    """Whole-atom integer DCT of the 1024^3 volume, x = vox - dc per atom as the
+    codec centres, forward and inverse, in both forms: butterfly (CUDA cores)
+    and IMMA (int8 tensor cores, hi/lo pieces). Every coefficient, dc and voxel
+    of the two forms is compared; the CPU leg times the C restatement of the
+    reference transform on a bounded sample of atoms and checks the device
+    outputs of those atoms."""
     import numpy as np
     import vc_gb300 as vc
     dims = (n, n, n)
+    centre = vc.DCT_ATOM_DC
     vol = vc.synth_device(n, n, n, vc.config_seed(3))
     coef = [vc.DeviceBuffer(n ** 3 * 4) for _ in range(2)]
     rec = [vc.DeviceBuffer(n ** 3) for _ in range(2)]
+    dcs = [vc.DeviceBuffer(n ** 3 // 32768) for _ in range(2)]
     res = {}
     for form, name in ((vc.DCT_BUTTERFLY, "butterfly"), (vc.DCT_IMMA, "imma")):
         fwd, inv = [], []
         for r in range(reps + 1):
-            s, redone = vc.dct_forward(vol, dims, centre, form, coef[form])
+            s, redone = vc.dct_forward(vol, dims, centre, form, coef[form], dcs[form])
             assert s == 0 and redone == 0, vc.last_error()
             if r or not reps:
                 fwd.append(vc.last_call_ms())
         for r in range(reps + 1):
-            s, redone = vc.dct_inverse(coef[form], dims, centre, form, rec[form])
+            s, redone = vc.dct_inverse(coef[form], dims, centre, form, rec[form], dcs[form])
             assert s == 0, vc.last_error()
             if r or not reps:
                 inv.append(vc.last_call_ms())
@@ -331,7 +334,9 @@ def config3_dct(n=1024, centre=128, reps=3, sample_atoms=256):
                      "forward_hbm_GBps": 5 * n ** 3 / (f / 1e3) / 1e9,
                      "inverse_voxel_GBps": n ** 3 / (i / 1e3) / 1e9,
                      "inverse_hbm_GBps": 5 * n ** 3 / (i / 1e3) / 1e9}
-    forms_equal = _equal_device(vc, coef[0], coef[1], n ** 3 * 4) and _equal_device(vc, rec[0], rec[1], n ** 3)
+    forms_equal = (_equal_device(vc, coef[0], coef[1], n ** 3 * 4) and _equal_device(vc, rec[0], rec[1], n ** 3)
+                   and _equal_device(vc, dcs[0], dcs[1], n ** 3 // 32768))
+    dc_host = dcs[1].download(n ** 3 // 32768)
     # CPU leg: the C restatement of the reference transform on a bounded sample of atoms
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oraclelib
@@ -353,9 +358,11 @@ def config3_dct(n=1024, centre=128, reps=3, sample_atoms=256):
         c_ref = np.empty(32768, np.int32)
         v_ref = np.empty(32768, np.uint8)
         t0 = time.perf_counter()
-        O.orc_fdct(host_vol.ctypes.data, centre, c_ref.ctypes.data)
-        O.orc_idct(c_ref.ctypes.data, centre, v_ref.ctypes.data)
+        dc = (int(host_vol.sum(dtype=np.int64)) + 16384) // 32768
+        O.orc_fdct(host_vol.ctypes.data, dc, c_ref.ctypes.data)
+        O.orc_idct(c_ref.ctypes.data, dc, v_ref.ctypes.data)
         t_cpu += time.perf_counter() - t0
+        ok = ok and dc == int(dc_host[a])
         c_dev = np.empty(32768, np.int32)
         L.vcg_copy(c_dev.ctypes.data, ctypes.c_void_p(coef[1].ptr + a * 32768 * 4), 32768 * 4)
         v_dev = np.empty((32, 32, 32), np.uint8)
@@ -364,9 +371,9 @@ def config3_dct(n=1024, centre=128, reps=3, sample_atoms=256):
                 L.vcg_copy(v_dev[z, y].ctypes.data,
                            ctypes.c_void_p(rec[1].ptr + ((az * 32 + z) * n + ay * 32 + y) * n + ax * 32), 32)
         ok = ok and bool(np.array_equal(c_dev, c_ref)) and bool(np.array_equal(v_dev.ravel(), v_ref))
-    for b in coef + rec + [vol]:
+    for b in coef + rec + dcs + [vol]:
         b.free()
-    return {"workload": f"{n}^3 u8 synthetic volume (seed 0x5EED0003), {na ** 3} atoms, centre {centre}, "
+    return {"workload": f"{n}^3 u8 synthetic volume (seed 0x5EED0003), {na ** 3} atoms, x = vox - dc per atom, "
                         "forward + inverse 3-D DCT-32",
             **res, "imma_vs_butterfly_forward_speedup": res["butterfly"]["forward_ms"] / res["imma"]["forward_ms"],
             "imma_vs_butterfly_inverse_speedup": res["butterfly"]["inverse_ms"] / res["imma"]["inverse_ms"],

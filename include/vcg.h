@@ -106,22 +106,26 @@ vc_status vcg_decode_atoms_noalloc(const uint8_t *payload_dev, size_t payload_by
 
 // Exact integer 3-D DCT-32 of every atom of a volume in device memory (no
 // counterpart in the reference's API: the reference's per-atom transform,
-// src/vc/vc.c:212-229, with `centre` as the value subtracted from every voxel,
-// e.g. 128 for u8 centred to signed). dims must be multiples of 32, centre in
-// [0, 255], both pointers 16-byte aligned device memory. Atoms are taken in
-// raster order (az, ay, ax); atom i's coefficients are coef[i*32768 ...] in
-// (kz, ky, kx) raster order. The inverse applies the reference's inverse
-// transform and adds centre back, clamped to [0, 255]. Both forms give the
-// reference's bits for every input: VCG_DCT_BUTTERFLY runs the even/odd
-// butterfly on the CUDA cores, VCG_DCT_IMMA runs each pass as int8 tensor-core
-// matrix products over hi/lo pieces; *redone (optional) receives the number of
-// atoms the IMMA form handed to the butterfly because an intermediate left its
-// piece range (0 for the forward transform).
+// src/vc/vc.c:212-229). `centre` is subtracted from every voxel (0..255, e.g.
+// 128 for u8 centred to signed) or, with VCG_DCT_ATOM_DC, each atom's dc
+// = (sum of its voxels + 16384) / 32768 as the codec uses (src/vc/vc.c:603):
+// the forward writes it to dc_dev[atom], the inverse reads it from there
+// (dc_dev: device memory, one byte per atom; ignored otherwise). dims must be
+// multiples of 32; coef_dev / vol_dev 16-byte aligned device memory. Atoms are
+// taken in raster order (az, ay, ax); atom i's coefficients are
+// coef[i*32768 ...] in (kz, ky, kx) raster order. The inverse applies the
+// reference's inverse transform and adds the centre back, clamped to [0, 255].
+// Both forms give the reference's bits for every input: VCG_DCT_BUTTERFLY runs
+// the even/odd butterfly on the CUDA cores, VCG_DCT_IMMA runs each pass as int8
+// tensor-core matrix products over hi/lo pieces; *redone (optional) receives
+// the number of atoms the IMMA form handed to the butterfly because an
+// intermediate left its piece range (always 0 for the forward transform).
 enum { VCG_DCT_BUTTERFLY = 0, VCG_DCT_IMMA = 1 };
+#define VCG_DCT_ATOM_DC (-1)
 vc_status vcg_dct_forward(const uint8_t *vol_dev, vc_dims dims, int centre, int form, int32_t *coef_dev,
-                          uint32_t *redone);
-vc_status vcg_dct_inverse(const int32_t *coef_dev, vc_dims dims, int centre, int form, uint8_t *vol_dev,
-                          uint32_t *redone);
+                          uint8_t *dc_dev, uint32_t *redone);
+vc_status vcg_dct_inverse(const int32_t *coef_dev, const uint8_t *dc_dev, vc_dims dims, int centre, int form,
+                          uint8_t *vol_dev, uint32_t *redone);
 
 // Seeded synthetic scroll-sheet volume (the benchmark workload) generated on
 // the device; byte-identical to the host generator in libvcsynth.

@@ -4,7 +4,10 @@
 // value, then along x, y and z the Q14 matrix CMATA with (acc + 2^13) >> 14
 // after every pass and i32 sums with wrap-around; the inverse applies CMATA^T
 // along x, y and z in the same way and adds the centre back, clamped to
-// [0, 255]. Coefficients of an atom are 32768 i32 in (kz, ky, kx) raster order.
+// [0, 255]. The centre is one value for every atom, or each atom's dc, the
+// rounded mean (sum + 16384) / 32768 of its voxels (src/vc/vc.c:603), as the
+// codec uses it. Coefficients of an atom are 32768 i32 in (kz, ky, kx) raster
+// order.
 //
 //   butterfly  CUDA cores: one CTA per atom, the recursive even/odd partial
 //              butterfly of dct32.cuh per line (344 multiplies per line).
@@ -41,7 +44,8 @@ struct DctJob {
     uint64_t nx, ny, nz;       // volume dims (multiples of 32)
     uint32_t ax, ay;           // atoms along x and y
     uint64_t n_atoms;
-    int32_t centre;
+    int32_t centre;            // >= 0: every atom's centre; < 0: each atom's dc
+    uint8_t *dc;               // per atom: written by the forward, read by the inverse (centre < 0)
     uint32_t *redone;          // atoms the imma form redid with the butterfly
 };
 
@@ -56,6 +60,45 @@ __device__ __forceinline__ void atom_xyz(const DctJob &J, uint64_t a, uint64_t &
 
 __device__ __forceinline__ uint8_t clamp_u8(int32_t v) { return (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v)); }
 
+// The 16-byte row pieces of atom a a thread loads: row i>>1 = (z, y), x0 = 16 (i & 1).
+__device__ __forceinline__ void load_rows(const DctJob &J, uint64_t bx, uint64_t by, uint64_t bz, uint4 (&w)[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int i = threadIdx.x + k * kDctThreads, row = i >> 1, z = row >> 5, y = row & 31;
+        w[k] = *reinterpret_cast<const uint4 *>(J.vol_in + ((bz + z) * J.ny + by + y) * J.nx + bx + (i & 1) * 16);
+    }
+}
+
+// Forward centre of atom a: the fixed centre, or the atom's dc from the voxels
+// every thread holds (written to J.dc[a]). Called by the whole CTA.
+__device__ int32_t fwd_centre(const DctJob &J, uint64_t a, const uint4 (&w)[8]) {
+    if (J.centre >= 0) return J.centre;
+    __shared__ uint32_t s_part[kDctThreads / 32];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        s = __dp4a(w[k].x, 0x01010101u, s);
+        s = __dp4a(w[k].y, 0x01010101u, s);
+        s = __dp4a(w[k].z, 0x01010101u, s);
+        s = __dp4a(w[k].w, 0x01010101u, s);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    uint32_t tot = 0;
+#pragma unroll
+    for (int i = 0; i < kDctThreads / 32; ++i) tot += s_part[i];
+    const int32_t dc = (int32_t)((tot + 16384u) >> 15);   // src/vc/vc.c:603
+    if (threadIdx.x == 0) J.dc[a] = (uint8_t)dc;
+    __syncthreads();
+    return dc;
+}
+
+__device__ __forceinline__ int32_t inv_centre(const DctJob &J, uint64_t a) {
+    return J.centre >= 0 ? J.centre : (int32_t)J.dc[a];
+}
+
 // ------------------------------------------------------------------ butterfly
 // One atom through the three passes with T as a 32 slabs x swizzled 32x32 i32
 // tile (element (z, y, x) at z*1024 + swz(y, x)): x and y per slab (warp per
@@ -66,16 +109,21 @@ __device__ void bf_atom(int32_t *T, const DctJob &J, uint64_t a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint64_t bx, by, bz;
     atom_xyz(J, a, bx, by, bz);
+    int32_t cen = 0;
     if (!INV) {
-        for (int i = tid; i < 2048; i += kDctThreads) {   // 16 voxels of row (z, y)
-            const int row = i >> 1, x0 = (i & 1) * 16, z = row >> 5, y = row & 31;
-            const uint4 w = *reinterpret_cast<const uint4 *>(J.vol_in + ((bz + z) * J.ny + by + y) * J.nx + bx + x0);
-            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+        uint4 w[8];
+        load_rows(J, bx, by, bz, w);
+        cen = fwd_centre(J, a, w);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {   // 16 voxels of row (z, y)
+            const int i = tid + k * kDctThreads, row = i >> 1, x0 = (i & 1) * 16, z = row >> 5, y = row & 31;
+            const uint32_t ws[4] = {w[k].x, w[k].y, w[k].z, w[k].w};
 #pragma unroll
             for (int b = 0; b < 16; ++b)
-                T[z * 1024 + swz(y, x0 + b)] = (int32_t)((ws[b >> 2] >> (8 * (b & 3))) & 0xFFu) - J.centre;
+                T[z * 1024 + swz(y, x0 + b)] = (int32_t)((ws[b >> 2] >> (8 * (b & 3))) & 0xFFu) - cen;
         }
     } else {
+        cen = inv_centre(J, a);
         const int4 *src = reinterpret_cast<const int4 *>(J.coef_in + a * 32768);
         for (int i = tid; i < 8192; i += kDctThreads) {
             const int4 w = src[i];
@@ -113,7 +161,7 @@ __device__ void bf_atom(int32_t *T, const DctJob &J, uint64_t a) {
             idct32_line(v, o);
 #pragma unroll
             for (int z = 0; z < 32; ++z)
-                J.vol_out[((bz + z) * J.ny + by + y) * J.nx + bx + x] = clamp_u8(o[z] + J.centre);
+                J.vol_out[((bz + z) * J.ny + by + y) * J.nx + bx + x] = clamp_u8(o[z] + cen);
         } else {
             fdct32_line(v, o);
             int32_t *dst = J.coef_out + a * 32768 + y * 32 + x;
@@ -189,12 +237,15 @@ __global__ void __launch_bounds__(kDctThreads, 1) k_dct_imma(DctJob J) {
         if (tid == 0) s_bad = 0;
         bool bad = false;
         // pass-0 input: line (z, y), element x
+        int32_t cen = 0;
         if (!INV) {
-            for (int i = tid; i < 2048; i += kDctThreads) {
-                const int row = i >> 1, half = i & 1, z = row >> 5, y = row & 31;
-                const uint4 w = *reinterpret_cast<const uint4 *>(J.vol_in + ((bz + z) * J.ny + by + y) * J.nx + bx +
-                                                                 half * 16);
-                const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+            uint4 wv[8];
+            load_rows(J, bx, by, bz, wv);
+            cen = fwd_centre(J, a, wv);
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const int i = tid + kk * kDctThreads, row = i >> 1, half = i & 1;
+                const uint32_t ws[4] = {wv[kk].x, wv[kk].y, wv[kk].z, wv[kk].w};
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     uint32_t pk[VP];
@@ -202,7 +253,7 @@ __global__ void __launch_bounds__(kDctThreads, 1) k_dct_imma(DctJob J) {
                     for (int j = 0; j < VP; ++j) pk[j] = 0;
 #pragma unroll
                     for (int i4 = 0; i4 < 4; ++i4) {
-                        const int32_t v = (int32_t)((ws[q] >> (8 * i4)) & 0xFFu) - J.centre;
+                        const int32_t v = (int32_t)((ws[q] >> (8 * i4)) & 0xFFu) - cen;
 #pragma unroll
                         for (int j = 0; j < VP; ++j) pk[j] |= piece<VP>(v, j) << (8 * i4);
                     }
@@ -212,6 +263,7 @@ __global__ void __launch_bounds__(kDctThreads, 1) k_dct_imma(DctJob J) {
                 }
             }
         } else {
+            cen = inv_centre(J, a);
             const int4 *src = reinterpret_cast<const int4 *>(J.coef_in + a * 32768);
             for (int i = tid; i < 8192; i += kDctThreads) {
                 const int4 w = src[i];
@@ -285,8 +337,8 @@ __global__ void __launch_bounds__(kDctThreads, 1) k_dct_imma(DctJob J) {
                             *reinterpret_cast<int2 *>(J.coef_out + a * 32768 + (k * 32 + la) * 32 + lb) =
                                 make_int2(o[0], o[1]);
                         } else {
-                            const uint32_t v2 = (uint32_t)clamp_u8(o[0] + J.centre) |
-                                                ((uint32_t)clamp_u8(o[1] + J.centre) << 8);
+                            const uint32_t v2 = (uint32_t)clamp_u8(o[0] + cen) |
+                                                ((uint32_t)clamp_u8(o[1] + cen) << 8);
                             *reinterpret_cast<uint16_t *>(J.vol_out + ((bz + k) * J.ny + by + la) * J.nx + bx + lb) =
                                 (uint16_t)v2;
                         }
@@ -309,17 +361,20 @@ using namespace vcg;
 
 #define VC_API extern "C" __attribute__((visibility("default")))
 
-static vc_status dct_run(const void *in, void *out, vc_dims dims, int centre, int form, int inverse,
+static vc_status dct_run(const void *in, void *out, uint8_t *dc, vc_dims dims, int centre, int form, int inverse,
                          uint32_t *redone) {
     if (!in || !out || !dims.nx || !dims.ny || !dims.nz || (dims.nx | dims.ny | dims.nz) & 31u ||
-        dims.nx > VC_MAX_DIM || dims.ny > VC_MAX_DIM || dims.nz > VC_MAX_DIM || centre < 0 || centre > 255 ||
+        dims.nx > VC_MAX_DIM || dims.ny > VC_MAX_DIM || dims.nz > VC_MAX_DIM || centre < VCG_DCT_ATOM_DC ||
+        centre > 255 || (centre == VCG_DCT_ATOM_DC && !dc) ||
         (form != VCG_DCT_BUTTERFLY && form != VCG_DCT_IMMA) || ((uintptr_t)in & 15u) || ((uintptr_t)out & 15u))
         return VC_ERR_RANGE;
     vcd_ctx *c = vcd_thread_ctx();
     if (!c) return VC_ERR_IO;
-    cudaPointerAttributes pa, pb;
+    cudaPointerAttributes pa, pb, pc;
     if (cudaPointerGetAttributes(&pa, in) != cudaSuccess || cudaPointerGetAttributes(&pb, out) != cudaSuccess ||
-        pa.type != cudaMemoryTypeDevice || pb.type != cudaMemoryTypeDevice) {
+        pa.type != cudaMemoryTypeDevice || pb.type != cudaMemoryTypeDevice ||
+        (centre == VCG_DCT_ATOM_DC &&
+         (cudaPointerGetAttributes(&pc, dc) != cudaSuccess || pc.type != cudaMemoryTypeDevice))) {
         cudaGetLastError();
         return VC_ERR_RANGE;
     }
@@ -342,6 +397,7 @@ static vc_status dct_run(const void *in, void *out, vc_dims dims, int centre, in
     J.ay = dims.ny / 32;
     J.n_atoms = (uint64_t)J.ax * J.ay * (dims.nz / 32);
     J.centre = centre;
+    J.dc = centre == VCG_DCT_ATOM_DC ? dc : nullptr;
     J.redone = (uint32_t *)p_red;
     const unsigned grid = (unsigned)(J.n_atoms < (uint64_t)g_dev.num_sms ? J.n_atoms : (uint64_t)g_dev.num_sms);
     cudaStream_t st = c->stream;
@@ -387,11 +443,11 @@ static vc_status dct_run(const void *in, void *out, vc_dims dims, int centre, in
 }
 
 VC_API vc_status vcg_dct_forward(const uint8_t *vol_dev, vc_dims dims, int centre, int form, int32_t *coef_dev,
-                                 uint32_t *redone) {
-    return dct_run(vol_dev, coef_dev, dims, centre, form, 0, redone);
+                                 uint8_t *dc_dev, uint32_t *redone) {
+    return dct_run(vol_dev, coef_dev, dc_dev, dims, centre, form, 0, redone);
 }
 
-VC_API vc_status vcg_dct_inverse(const int32_t *coef_dev, vc_dims dims, int centre, int form, uint8_t *vol_dev,
-                                 uint32_t *redone) {
-    return dct_run(coef_dev, vol_dev, dims, centre, form, 1, redone);
+VC_API vc_status vcg_dct_inverse(const int32_t *coef_dev, const uint8_t *dc_dev, vc_dims dims, int centre, int form,
+                                 uint8_t *vol_dev, uint32_t *redone) {
+    return dct_run(coef_dev, vol_dev, const_cast<uint8_t *>(dc_dev), dims, centre, form, 1, redone);
 }

@@ -84,20 +84,24 @@ class Server:
         self.close()
 
 
-DCT_BUTTERFLY, DCT_IMMA = 0, 1
+DCT_BUTTERFLY, DCT_IMMA, DCT_ATOM_DC = 0, 1, -1
 
 
-def dct_forward(vol, dims, centre, form, coef):
-    """vcg_dct_forward: vol, coef DeviceBuffers; dims (nx, ny, nz). Returns (status, atoms redone)."""
+def dct_forward(vol, dims, centre, form, coef, dc=None):
+    """vcg_dct_forward: vol, coef (and dc, for centre DCT_ATOM_DC) DeviceBuffers;
+    dims (nx, ny, nz). Returns (status, atoms redone)."""
     r = ctypes.c_uint32()
-    s = lib().vcg_dct_forward(vol.ptr, Dims(*dims), centre, form, coef.ptr, ctypes.byref(r))
+    s = lib().vcg_dct_forward(vol.ptr, Dims(*dims), centre, form, coef.ptr, dc.ptr if dc else None,
+                              ctypes.byref(r))
     return s, r.value
 
 
-def dct_inverse(coef, dims, centre, form, vol):
-    """vcg_dct_inverse: coef, vol DeviceBuffers; dims (nx, ny, nz). Returns (status, atoms redone)."""
+def dct_inverse(coef, dims, centre, form, vol, dc=None):
+    """vcg_dct_inverse: coef, vol (and dc, for centre DCT_ATOM_DC) DeviceBuffers;
+    dims (nx, ny, nz). Returns (status, atoms redone)."""
     r = ctypes.c_uint32()
-    s = lib().vcg_dct_inverse(coef.ptr, Dims(*dims), centre, form, vol.ptr, ctypes.byref(r))
+    s = lib().vcg_dct_inverse(coef.ptr, dc.ptr if dc else None, Dims(*dims), centre, form, vol.ptr,
+                              ctypes.byref(r))
     return s, r.value
 
 
@@ -163,8 +167,8 @@ def lib():
         L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
         L.vcg_batch_shape.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.vcg_set_rc_scalar_warps.argtypes = [ctypes.c_int]
-        L.vcg_dct_forward.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
-        L.vcg_dct_inverse.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
+        L.vcg_dct_forward.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, P, ctypes.POINTER(ctypes.c_uint32)]
+        L.vcg_dct_inverse.argtypes = [P, P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
         L.vcg_server_create.restype = P
         L.vcg_server_create.argtypes = [P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int]
         L.vcg_server_submit.restype = ctypes.c_int64
