@@ -96,39 +96,86 @@ class Dist:
 
 # ---------------------------------------------------------------- clocks
 class Clocks:
+    """SM clock and clock-event (throttle) reasons sampled during a timed region:
+    NVML read-only queries every 5 ms from a thread (libnvidia-ml through
+    ctypes), else nvidia-smi every 200 ms."""
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap",
+               0x80: "hw_power_brake_slowdown"}
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index=0):
-        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-        self.p = None
+        self.samples, self.mask, self.max_mhz = [], 0, None
+        self.stop_ev = threading.Event()
+        self.p = self.t = None
+        self.nvml = self._nvml(gpu_index)
+        if self.nvml:
+            self.t = threading.Thread(target=self._loop, daemon=True)
+            self.t.start()
+        else:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            try:
+                self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                           "-i", str(gpu_index), "-lms", "200"], stdout=self.f,
+                                          stderr=subprocess.DEVNULL)
+            except OSError:
+                self.p = None
+
+    def _nvml(self, idx):
         try:
-            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                       "-i", str(gpu_index), "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
-        except OSError:
-            self.p = None
+            L = ctypes.CDLL("libnvidia-ml.so.1")
+            if L.nvmlInit_v2() != 0:
+                return None
+            h = ctypes.c_void_p()
+            if L.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(idx), ctypes.byref(h)) != 0:
+                return None
+            mx = ctypes.c_uint()
+            if L.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            reasons = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                L.nvmlDeviceGetCurrentClocksThrottleReasons
+            return L, h, reasons
+        except (OSError, AttributeError):
+            return None
+
+    def _loop(self):
+        L, h, reasons = self.nvml
+        mhz, r = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop_ev.is_set():
+            if L.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0:
+                self.samples.append(float(mhz.value))
+            if reasons(h, ctypes.byref(r)) == 0:
+                self.mask |= r.value
+            time.sleep(0.005)
 
     def stop(self):
+        if self.t:
+            self.stop_ev.set()
+            self.t.join()
+            return {"sm_mhz": statistics.median(self.samples) if self.samples else None, "sm_max_mhz": self.max_mhz,
+                    "reasons": sorted(n for bit, n in self.REASONS.items() if self.mask & bit),
+                    "samples": len(self.samples), "source": "nvml, 5 ms"}
         if self.p:
             self.p.terminate()
             self.p.wait()
-        self.f.flush()
         rows = []
-        with open(self.f.name) as f:
-            for line in f:
-                parts = [x.strip() for x in line.split(",")]
-                if len(parts) >= 9:
-                    rows.append(parts)
-        os.unlink(self.f.name)
+        if self.p:
+            self.f.flush()
+            with open(self.f.name) as f:
+                for line in f:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+            os.unlink(self.f.name)
         if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "source": "nvidia-smi, 200 ms"}
 
 
 def dram_traffic(kernel, units):
