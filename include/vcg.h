@@ -46,7 +46,7 @@ void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads);
 // atoms decoded in lockstep have the highest throughput. Atoms are decoded one
 // per warp while that makes at most w warps per SM sub-partition (4 per SM),
 // else in warps of the smallest power of two that keeps to about one warp per
-// sub-partition. w <= 0 restores the default (4).
+// sub-partition. w <= 0 restores the default (16).
 void vcg_set_rc_scalar_warps(int w);
 
 // Decode server: continuous batching against one resident archive. Requests

@@ -77,8 +77,9 @@ struct BatchShape {              // tunables the autotuner chooses among
 // scalar decoder, whose latency per atom is the lowest; a warp of several atoms
 // runs them in lockstep, which costs more decision steps per atom but issues
 // each instruction for all of them. One atom per warp while that makes at most
-// `scalar_warps` warps per SM sub-partition (4 per SM), else the smallest power
-// of two that keeps to about one warp per sub-partition, at most 32.
+// `scalar_warps` warps per SM sub-partition (4 per SM; measured on GB300, the
+// scalar decoder wins up to about 16 per sub-partition), else the smallest
+// power of two that keeps to about one warp per sub-partition, at most 32.
 __host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms, uint32_t scalar_warps) {
     const uint64_t slots = 4ull * sms;
     if (n_atoms <= (uint64_t)scalar_warps * slots) return 1;
@@ -86,7 +87,7 @@ __host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms,
     while (g < 32 && (uint64_t)g * slots < n_atoms) g <<= 1;
     return g;
 }
-constexpr uint32_t kRcScalarWarpsDefault = 4;
+constexpr uint32_t kRcScalarWarpsDefault = 16;
 // policy of the plain decode path (vcg_set_rc_scalar_warps)
 uint32_t rc_scalar_warps();
 void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s);

@@ -232,23 +232,23 @@ __device__ __forceinline__ int rc_decode_levels_warp(const uint8_t *src, uint32_
             const uint32_t sh = range < kTop ? 8u : 0u;
             range <<= sh;
             s.shift(code, sh);
-            const bool live = p < eob && !bad;
-            const bool nz = one && live;
-            const bool empty = s.nb == 0 && live;
-            if (!__any_sync(kFull, nz || empty)) continue;
-            s.refill_if(empty);
+            const bool nz = one && p < eob && !bad;
+            ls_keep(s);
             if (!__any_sync(kFull, nz)) continue;
+            // unary magnitude: every lane with a nonzero takes step 0, so it needs
+            // no vote; the escape vote is taken with the last step
             uint32_t m = 0;
-            bool go = nz;
+            bool go = nz, esc = false;
 #pragma unroll
             for (int k = 0; k < 12; ++k) {
-                if (!__any_sync(kFull, go)) break;
+                if (k > 0 && !__any_sync(kFull, go)) break;
                 const bool more = ls_ctx(go, code, range, mag[k], s);
                 m = (go && !more) ? (uint32_t)k + 1u : m;
                 go = go && more;
                 ls_keep(s);
+                if (k == 11) esc = __any_sync(kFull, go);
             }
-            if (__any_sync(kFull, go)) {   // escape: EG0 tail in bypass bits (rare)
+            if (esc) {   // escape: EG0 tail in bypass bits (rare)
                 uint32_t ones = 0, x = 1, rem = 0;
                 bool pre = go, suf = false;
                 while (__any_sync(kFull, pre || suf)) {
