@@ -25,8 +25,9 @@ __device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t 
 }
 
 // Tile of one PRESENT atom after the inverse passes along x and y: levels
-// scattered into T (32 slabs x swizzled 32x32, i32), dequantised while each
-// slab is loaded, then one warp per slab (lane per line). Ends with a barrier.
+// dequantised as they are scattered into T (32 slabs x swizzled 32x32, i32;
+// only the nonzero levels are touched), then one warp per slab (lane per
+// line). Ends with a barrier.
 template <int NT>
 __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, const vcd_atom &e, uint32_t c,
                                              const uint32_t *src, const uint16_t *scan, const uint32_t *band_start,
@@ -38,13 +39,16 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
     if (c & kEntOverflow) {
         // slow path for streams whose list exceeded its capacity
         if (tid == 0)
-            rc_decode_levels_lane(arc + e.off + 1, e.len - 1, band_start,
-                                  [&](uint32_t p, uint32_t lv) { T[tile_idx(scan[p])] = (int16_t)lv; });
+            rc_decode_levels_lane(arc + e.off + 1, e.len - 1, band_start, [&](uint32_t p, uint32_t lv) {
+                const uint32_t r = scan[p];
+                T[tile_idx(r)] = dequant((int16_t)lv, r, dqs, dqb, alt);
+            });
     } else {
         const uint32_t n = c & kEntMask;
         for (uint32_t i = tid; i < n; i += NT) {
-            uint32_t w = src[i];
-            T[tile_idx(__ldg(scan + (w & 0xFFFFu)))] = (int16_t)(w >> 16);
+            const uint32_t w = src[i];
+            const uint32_t r = __ldg(scan + (w & 0xFFFFu));
+            T[tile_idx(r)] = dequant((int16_t)(w >> 16), r, dqs, dqb, alt);
         }
     }
     __syncthreads();
@@ -54,11 +58,10 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
         int any = 0;
 #pragma unroll
         for (int kx = 0; kx < 32; ++kx) {
-            int32_t l = S[swz(lane, kx)];
-            v[kx] = dequant(l, (uint32_t)(kz * 1024 + lane * 32 + kx), dqs, dqb, alt);
+            v[kx] = S[swz(lane, kx)];
             any |= v[kx];
         }
-        if (__any_sync(0xFFFFFFFFu, any)) {
+        if (__any_sync(0xFFFFFFFFu, any)) {   // an all-zero slab stays zero
             idct32_line(v, o);
 #pragma unroll
             for (int x = 0; x < 32; ++x) S[swz(lane, x)] = o[x];
@@ -69,9 +72,6 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
             __syncwarp();
 #pragma unroll
             for (int y = 0; y < 32; ++y) S[swz(y, lane)] = o[y];
-        } else {
-#pragma unroll
-            for (int x = 0; x < 32; ++x) S[swz(lane, x)] = 0;
         }
         __syncwarp();
     }

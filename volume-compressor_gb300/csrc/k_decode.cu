@@ -23,7 +23,7 @@
 
 namespace vcg {
 
-constexpr int kIdctThreads = 256;
+constexpr int kIdctThreads = 512;   // 16 warps per atom (measured faster than 8 on GB300)
 constexpr size_t kIdctSmem = 32768 * sizeof(int32_t);
 
 __global__ void k_caps(DecodeJob J) {

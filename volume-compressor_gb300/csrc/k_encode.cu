@@ -75,15 +75,58 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
     for (int i = tid; i < 1024; i += kFwdThreads) alt[i] = J.alt_mask[i];
     int cur_lod = -1;
 
+    // quantise coefficient cf at (kz, ky, kx = lane) and scatter its level to scan order
+    auto quant_scatter = [&](int32_t cf, int kz, int ky) {
+        const uint32_t f = (uint32_t)(kz + ky + lane);
+        const uint32_t r = (uint32_t)(kz * 1024 + ky * 32 + lane);
+        const uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
+        const uint32_t mag = cf < 0 ? 0u - (uint32_t)cf : (uint32_t)cf;
+        const float fa = __int2float_rn((int32_t)mag);
+        int32_t level = 0;
+        if (fa >= qdz[cls]) {
+            level = __float2int_rz(__fadd_rn(__fmul_rn(__fsub_rn(fa, qdz[cls]), qrr[cls]), 1.0f));
+            if (level > 32767) level = 32767;
+        }
+        if (level) {
+            int sub = (int)f - kz - 31;
+            uint32_t p = (uint32_t)rank[f * 32 + kz] + (uint32_t)ky - (uint32_t)(sub > 0 ? sub : 0);
+            L[p] = (int16_t)(cf < 0 ? -level : level);
+        }
+    };
+
     for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
         int lod;
         uint32_t az, ay, ax;
-        J.lay.coords(J.first + t, lod, az, ay, ax);
+        const uint64_t ca = J.first + t;   // canonical index
+        J.lay.coords(ca, lod, az, ay, ax);
         if (lod != cur_lod) {   // uniform across the CTA: quantiser constants of this LOD
             for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q[lod].dz[i]; qrr[i] = J.q[lod].rr[i]; }
             cur_lod = lod;
             __syncthreads();
         }
+        const bool cached = J.coef && ca < J.coef_n;
+        int32_t *cptr = cached ? J.coef + ca * 32768ull : nullptr;
+        int4 *L4 = reinterpret_cast<int4 *>(L);
+        int32_t dc;
+        if (cached && !J.coef_store) {
+            // the transform of this atom was kept: quantise straight from it
+            const uint32_t dcz = J.coef_dc[ca];
+            if (dcz & kMetaZero) {
+                if (tid == 0) J.meta[t] = kMetaZero;
+                continue;
+            }
+            dc = (int32_t)(dcz & 0xFFu);
+            for (int i = tid; i < 32768 * 2 / 16; i += kFwdThreads) L4[i] = make_int4(0, 0, 0, 0);
+            __syncthreads();
+            for (int ky = warp; ky < 32; ky += kFwdThreads / 32) {
+                int32_t o[32];
+#pragma unroll
+                for (int kz = 0; kz < 32; ++kz) o[kz] = __ldcs(cptr + kz * 1024 + ky * 32 + lane);
+#pragma unroll
+                for (int kz = 0; kz < 32; ++kz) quant_scatter(o[kz], kz, ky);
+            }
+            __syncthreads();
+        } else {
         const uint8_t *vol = J.vol[lod];
         const uint32_t nx = J.dims[lod][0], ny = J.dims[lod][1], nz = J.dims[lod][2];
         // rows r = tid + 256 j: z = r >> 5, y = r & 31 (lane)
@@ -97,7 +140,6 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
             for (int i = 0; i < 8; ++i) s = __dp4a(w[j][i], 0x01010101u, s);
         }
         // zero the scan-order level buffer while the sum reduces
-        int4 *L4 = reinterpret_cast<int4 *>(L);
         for (int i = tid; i < 32768 * 2 / 16; i += kFwdThreads) L4[i] = make_int4(0, 0, 0, 0);
 #pragma unroll
         for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
@@ -107,11 +149,15 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
 #pragma unroll
         for (int i = 0; i < kFwdThreads / 32; ++i) sum += red[i];
         if (sum == 0) {   // all-zero atom: no payload (src/vc/vc.c:601)
-            if (tid == 0) J.meta[t] = kMetaZero;
+            if (tid == 0) {
+                J.meta[t] = kMetaZero;
+                if (cached) J.coef_dc[ca] = kMetaZero;
+            }
             __syncthreads();
             continue;
         }
-        const int32_t dc = (int32_t)((sum + 16384u) / 32768u);
+        dc = (int32_t)((sum + 16384u) / 32768u);
+        if (cached && tid == 0) J.coef_dc[ca] = (uint32_t)dc;
         // pass along x for the thread's 4 rows, straight from registers
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -142,27 +188,15 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
 #pragma unroll
             for (int z = 0; z < 32; ++z) v[z] = T[z * 1024 + swz(ky, lane)];
             fdct32_line(v, o);
+            if (cached) {
 #pragma unroll
-            for (int kz = 0; kz < 32; ++kz) {
-                const int32_t cf = o[kz];
-                const uint32_t f = (uint32_t)(kz + ky + lane);
-                const uint32_t r = (uint32_t)(kz * 1024 + ky * 32 + lane);
-                const uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
-                const uint32_t mag = cf < 0 ? 0u - (uint32_t)cf : (uint32_t)cf;
-                const float fa = __int2float_rn((int32_t)mag);
-                int32_t level = 0;
-                if (fa >= qdz[cls]) {
-                    level = __float2int_rz(__fadd_rn(__fmul_rn(__fsub_rn(fa, qdz[cls]), qrr[cls]), 1.0f));
-                    if (level > 32767) level = 32767;
-                }
-                if (level) {
-                    int sub = (int)f - kz - 31;
-                    uint32_t p = (uint32_t)rank[f * 32 + kz] + (uint32_t)ky - (uint32_t)(sub > 0 ? sub : 0);
-                    L[p] = (int16_t)(cf < 0 ? -level : level);
-                }
+                for (int kz = 0; kz < 32; ++kz) cptr[kz * 1024 + ky * 32 + lane] = o[kz];
             }
+#pragma unroll
+            for (int kz = 0; kz < 32; ++kz) quant_scatter(o[kz], kz, ky);
         }
         __syncthreads();
+        }
         // compaction in scan order: thread owns positions [128 tid, 128 tid + 128)
         const uint4 *Lv = reinterpret_cast<const uint4 *>(L + tid * 128);
         uint32_t cnt = 0;

@@ -49,6 +49,13 @@ struct FwdJob {
     const uint32_t *alt_mask;
     uint32_t *ent;               // per atom VCD_MAX_ENTRIES slots: scan position | level << 16
     uint32_t *meta;              // per atom
+    // coefficient cache of canonical atoms [0, coef_n): 32768 i32 per atom in
+    // (kz, ky, kx) raster order, and dc | kMetaZero per atom; coef_store != 0
+    // fills it, else atoms below coef_n are quantised from it
+    int32_t *coef;
+    uint32_t *coef_dc;
+    uint64_t coef_n;
+    int coef_store;
 };
 
 struct RcJob {

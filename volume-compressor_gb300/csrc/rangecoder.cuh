@@ -376,15 +376,18 @@ __device__ __forceinline__ uint32_t rc_encode_levels_warp(const uint32_t *ent, u
             if (!__any_sync(kFull, nz)) continue;
             const int32_t lv = (int16_t)(cur >> 16);
             const uint32_t m = (uint32_t)(lv < 0 ? -lv : lv);
-            bool go = nz;
+            // every lane with a nonzero takes unary step 0, so it needs no vote;
+            // the escape vote is taken with the last step
+            bool go = nz, esc = false;
 #pragma unroll
             for (int k = 0; k < 12; ++k) {
-                if (!__any_sync(kFull, go)) break;
+                if (k > 0 && !__any_sync(kFull, go)) break;
                 const bool one = m > (uint32_t)k + 1u;   // unary: 1 while more remains
                 enc_ctx(go, one, e, mag[k]);
                 go = go && one;
+                if (k == 11) esc = __any_sync(kFull, go);
             }
-            if (__any_sync(kFull, go)) {   // escape: EG0 of m - 12 in bypass bits (rare)
+            if (esc) {   // escape: EG0 of m - 12 in bypass bits (rare)
                 const uint32_t x1 = go ? m - 11u : 2u;
                 const uint32_t nb = 31u - __clz(x1);
                 uint32_t step = 0;

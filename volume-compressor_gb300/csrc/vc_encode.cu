@@ -39,6 +39,11 @@ struct EncState {
     unsigned long long *red;
     vcd_quant *qtab;          // device, per LOD
     vcd_quant qh;             // host staging
+    // LOD0 forward transform kept across passes (null when it does not fit)
+    int32_t *coef;
+    uint32_t *coef_dc;
+    uint64_t coef_n;
+    bool coef_valid;
 };
 
 // Quantiser constants of `lod` at q, into the device table.
@@ -65,6 +70,11 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
         F.alt_mask = g_dev.tables->alt_mask;
         F.ent = S.ent;
         F.meta = S.meta;
+        F.coef = S.coef;
+        F.coef_dc = S.coef_dc;
+        F.coef_n = S.coef_n;
+        F.coef_store = !S.coef_valid;
+        const bool from_cache = S.coef && S.coef_valid && c0 + n <= S.coef_n;
         const bool prof = vcd_prof_on();
         if (prof) cudaEventRecord(S.c->ev[4], S.c->stream);
         launch_fwd(F, g_dev.num_sms, S.c->stream);
@@ -87,11 +97,15 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
         }
         if (prof) cudaEventRecord(S.c->ev[5], S.c->stream);
         launch_rc_encode(R, write, S.c->stream);
+        if (S.coef && c0 < S.coef_n && c0 + n >= S.coef_n) S.coef_valid = true;   // LOD0 transform kept
         if (prof) {
             cudaEventRecord(S.c->ev[1], S.c->stream);
             cudaEventSynchronize(S.c->ev[1]);
             // forward: volume bytes in (the lists it writes are scratch, not counted)
-            vcd_prof_add("fwd_dct_quant", vcd_elapsed(S.c->ev[4], S.c->ev[5]), 1, n * 32768ull, 0, n);
+            if (from_cache)   // coefficients in, lists out (scratch, not counted)
+                vcd_prof_add("quant_cached", vcd_elapsed(S.c->ev[4], S.c->ev[5]), 1, n * 131072ull, 0, n);
+            else
+                vcd_prof_add("fwd_dct_quant", vcd_elapsed(S.c->ev[4], S.c->ev[5]), 1, n * 32768ull, 0, n);
             vcd_prof_add(write ? "rc_encode_write" : "rc_encode_size", vcd_elapsed(S.c->ev[5], S.c->ev[1]), 1, 0,
                          0, n);
         }
@@ -158,6 +172,17 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     S.pos = (uint64_t *)p;
     CK(vcd_scratch(c, VCD_BUF_RED, 64, &p), "totals");
     S.red = (unsigned long long *)p;
+    {   // keep LOD0's forward transform (128 KiB per atom) when it takes at most half the free memory
+        size_t fr = 0, tot = 0;
+        const size_t cb = (size_t)na0 * 131072 + (size_t)na0 * 4 + 64;
+        if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && (c->cap[VCD_BUF_COEF] >= cb || cb <= fr / 2) &&
+            vcd_scratch(c, VCD_BUF_COEF, cb, &p) == cudaSuccess) {
+            S.coef = (int32_t *)p;
+            S.coef_dc = (uint32_t *)((uint8_t *)p + (size_t)na0 * 131072);
+            S.coef_n = na0;
+        }
+        cudaGetLastError();
+    }
 
     // ---- rate control on LOD0 (bisection over float bit patterns of [0.05, 4096])
     uint32_t lo = b_of(0.05f), hi = b_of(4096.0f);
@@ -274,6 +299,15 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     free(hd);
     if (e != cudaSuccess) { free(res); vcd_set_error("archive assembly", e); return vcd_status_of(e); }
     c->last_ms = vcd_elapsed(c->ev[6], c->ev[7]);
+    {   // a large transform cache is not kept between encodes (more than 1/8 of the device memory)
+        size_t fr = 0, tot = 0;
+        if (c->buf[VCD_BUF_COEF] && cudaMemGetInfo(&fr, &tot) == cudaSuccess && c->cap[VCD_BUF_COEF] > tot / 8) {
+            cudaFree(c->buf[VCD_BUF_COEF]);
+            c->buf[VCD_BUF_COEF] = NULL;
+            c->cap[VCD_BUF_COEF] = 0;
+        }
+        cudaGetLastError();
+    }
     *out = res;
     *out_len = total;
     return 0;
