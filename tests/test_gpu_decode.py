@@ -191,3 +191,39 @@ def test_truncated_archive_matches_oracle(vc, oracle, gpu, golden):
             assert s1 == s2, (cut, lod)
             if s1 == 0:
                 assert (g == r).all()
+
+
+def test_large_decode_into_pinned_memory_overlaps_copy_out(vc, gpu):
+    """A LOD0 decode of >= 64 MiB into pinned host memory takes the path that
+    copies each transformed slab out while the next one is transformed; it must
+    give the same bytes and statuses as the plain path into pageable memory,
+    also when an atom in the middle of the volume is malformed (then only the
+    atoms before it may be written)."""
+    import ctypes
+    import struct
+    n = 512
+    dv = vc.synth_device(n, n, n, vc.config_seed(2))
+    s, data = vc.encode_q(dv, 10.0, [2.0 * 0.6 ** l for l in range(8)], on_device=(n, n, n))
+    assert s == 0
+    dv.free()
+    L = vc.lib()
+    pinned = L.vcg_alloc_host(n ** 3)
+    assert pinned
+    try:
+        pv = (ctypes.c_uint8 * (n ** 3)).from_address(pinned)
+        view = np.frombuffer(pv, np.uint8)
+        bad = bytearray(data)
+        so = _slot_offset(bad, 0, 8, 5, 9)   # atom (az, ay, ax) = (8, 5, 9): mid-volume
+        struct.pack_into("<I", bad, so + 8, len(bad))
+        for arc_bytes in (bytes(data), bytes(bad)):
+            a = vc.Archive(arc_bytes)
+            ref = np.full(n ** 3, 0x3C, np.uint8)
+            s_ref, _ = a.decode_lod(0, ref.reshape(n, n, n))
+            view[:] = 0x3C
+            d = vc.Dims()
+            s_pin = L.vc_decode_lod(a.h, 0, pinned, ctypes.byref(d))
+            assert s_pin == s_ref
+            assert np.array_equal(view, ref)
+        assert s_ref == vc.VC_ERR_FORMAT
+    finally:
+        L.vcg_free_host(pinned)

@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
     for (int i = tid; i < 1024; i += kIdctThreads) alt[i] = J.alt_mask[i];
     __syncthreads();
 
-    for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
+    for (uint64_t t = J.t_lo + blockIdx.x; t < J.t_hi; t += gridDim.x) {
         uint32_t az, ay, ax;
         box_atom(J, t, az, ay, ax);
         const vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
@@ -173,24 +173,32 @@ void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cu
     k_scan_u64<<<1, 1024, 0, s>>>(v, n, base, total);
 }
 
-void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s) {
+static void idct_attr() {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_idct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIdctSmem);
         attr = true;
     }
-    if (!J.n_atoms) return;
-    launch_rc(J, num_sms, s);
-    uint64_t grid = J.n_atoms < (uint64_t)num_sms ? J.n_atoms : (uint64_t)num_sms;
-    k_idct<<<(unsigned)grid, kIdctThreads, kIdctSmem, s>>>(J);
 }
 
-void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_idct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIdctSmem);
-        attr = true;
-    }
+void launch_idct(const DecodeJob &J, int num_sms, cudaStream_t s, uint64_t t_lo, uint64_t t_hi) {
+    idct_attr();
+    if (t_hi <= t_lo) return;
+    DecodeJob Jr = J;
+    Jr.t_lo = t_lo;
+    Jr.t_hi = t_hi;
+    const uint64_t n = t_hi - t_lo;
+    const uint64_t grid = n < (uint64_t)num_sms ? n : (uint64_t)num_sms;
+    k_idct<<<(unsigned)grid, kIdctThreads, kIdctSmem, s>>>(Jr);
+}
+
+void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s) {
+    if (!J.n_atoms) return;
+    launch_rc(J, num_sms, s);
+    launch_idct(J, num_sms, s, 0, J.n_atoms);
+}
+
+void launch_decode_front(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev) {
     if (ev) cudaEventRecord(ev->ev[0], s);
     unsigned nb = (unsigned)((J.n_atoms + 127) / 128);
     if (J.n_atoms) {
@@ -200,10 +208,11 @@ void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageE
     if (ev) cudaEventRecord(ev->ev[1], s);
     if (J.n_atoms) launch_rc(J, num_sms, s);
     if (ev) cudaEventRecord(ev->ev[2], s);
-    if (J.n_atoms) {
-        uint64_t grid = J.n_atoms < (uint64_t)num_sms ? J.n_atoms : (uint64_t)num_sms;
-        k_idct<<<(unsigned)grid, kIdctThreads, kIdctSmem, s>>>(J);
-    }
+}
+
+void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev) {
+    launch_decode_front(J, num_sms, s, ev);
+    launch_idct(J, num_sms, s, 0, J.n_atoms);
     if (ev) cudaEventRecord(ev->ev[3], s);
 }
 

@@ -30,6 +30,7 @@ struct DecodeJob {
     uint32_t *err;               // lowest malformed box atom (atomicMin)
     unsigned long long *nnz_total;   // coefficient-list entries written (sum over atoms)
     uint32_t band_start[9];      // first scan position of each significance band
+    uint64_t t_lo, t_hi;         // box atoms the inverse transform launch covers
 };
 
 // Optional per-stage events: ev[0] before the list placement, ev[1] before the
@@ -93,6 +94,10 @@ uint32_t rc_scalar_warps();
 void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s);
 
 void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev);
+// The decode in two halves: list placement + range decode (events ev[0..2]),
+// then the inverse transform of box atoms [t_lo, t_hi).
+void launch_decode_front(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev);
+void launch_idct(const DecodeJob &J, int num_sms, cudaStream_t s, uint64_t t_lo, uint64_t t_hi);
 // Range decode + inverse transform only: J.ent_off must already hold each
 // atom's list offset (each list can take VCD_MAX_ENTRIES entries).
 void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s);

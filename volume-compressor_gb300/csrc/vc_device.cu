@@ -70,6 +70,10 @@ static void ctx_free(void *p) {
         if (c->buf[i]) cudaFree(c->buf[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+    if (c->copy_stream) {
+        for (int i = 0; i < 8; ++i) cudaEventDestroy(c->chunk_ev[i]);
+        cudaStreamDestroy(c->copy_stream);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     free(c);
 }
@@ -265,10 +269,61 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
     cudaMemsetAsync(p_err, 0xFF, 4, c->stream);
     StageEvents ev;
     memcpy(ev.ev, c->ev, sizeof ev.ev);
-    launch_decode(J, g_dev.num_sms, c->stream, &ev);
     uint64_t ctl_h[2] = {0xFFFFFFFFull, 0};
-    cudaMemcpyAsync(ctl_h, p_ctl, 16, cudaMemcpyDeviceToHost, c->stream);
-    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) {
+    // Large outputs to pinned host memory: the inverse transform runs in slabs of
+    // atom layers and each finished slab is copied out on a second stream while
+    // the next one is transformed. The range decode finishes first, so a stream
+    // with a malformed atom is known before any byte reaches the caller.
+    // (only when every atom of the box is decoded: a box cut short by a bad
+    // payload range keeps the exact per-atom copy below)
+    bool piped = false;
+    const uint64_t layer = (uint64_t)r->bnx * r->bny, layers = layer ? n / layer : 0;
+    if (out_host && out_bytes >= (64ull << 20) && n == box_atoms && layers * layer == n && layers >= 2) {
+        cudaPointerAttributes pa;
+        piped = cudaPointerGetAttributes(&pa, out_host) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        if (piped && !c->copy_stream) {
+            if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+                c->copy_stream = NULL;
+                piped = false;
+            } else {
+                for (int i = 0; i < 8; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
+            }
+        }
+    }
+    if (piped) {
+        launch_decode_front(J, g_dev.num_sms, c->stream, &ev);
+        cudaMemcpyAsync(ctl_h, p_ctl, 16, cudaMemcpyDeviceToHost, c->stream);
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+            vcd_set_error("decode kernels", e);
+            return vcd_status_of(e);
+        }
+        if ((uint32_t)ctl_h[0] < n) {   // malformed: whole transform, then the partial copy below
+            launch_idct(J, g_dev.num_sms, c->stream, 0, n);
+            cudaEventRecord(ev.ev[3], c->stream);
+            piped = false;
+        } else {
+            const uint64_t plane = (uint64_t)J.ox * J.oy;
+            const uint64_t per = (layers + 7) / 8;
+            int k = 0;
+            for (uint64_t l0 = 0; l0 < layers; l0 += per, ++k) {
+                const uint64_t l1 = l0 + per < layers ? l0 + per : layers;
+                launch_idct(J, g_dev.num_sms, c->stream, l0 * layer, l1 * layer);
+                cudaEventRecord(c->chunk_ev[k], c->stream);
+                const uint64_t zlo = (r->baz + l0) * 32 > r->z0 ? (r->baz + l0) * 32 : r->z0;
+                const uint64_t zhi = (r->baz + l1) * 32 < r->z1 ? (r->baz + l1) * 32 : r->z1;
+                cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0);
+                cudaMemcpyAsync(out_host + (zlo - r->z0) * plane, (uint8_t *)p_out + (zlo - r->z0) * plane,
+                                (zhi - zlo) * plane, cudaMemcpyDeviceToHost, c->copy_stream);
+            }
+            cudaEventRecord(ev.ev[3], c->stream);
+        }
+    } else {
+        launch_decode(J, g_dev.num_sms, c->stream, &ev);
+        cudaMemcpyAsync(ctl_h, p_ctl, 16, cudaMemcpyDeviceToHost, c->stream);
+    }
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess || (piped && (e = cudaStreamSynchronize(c->copy_stream)) != cudaSuccess) ||
+        (e = cudaGetLastError()) != cudaSuccess) {
         vcd_set_error("decode kernels", e);
         return vcd_status_of(e);
     }
@@ -283,7 +338,7 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
     const uint32_t err_h = (uint32_t)ctl_h[0];
     const uint64_t good = err_h < n ? err_h : n;   // atoms written before the first bad one
     const int status = (good < box_atoms) ? 1 /*VC_ERR_FORMAT*/ : 0;
-    if (!out_host) return status;
+    if (!out_host || piped) return status;   // piped: already copied out
     if (!status) {
         if ((e = cudaMemcpyAsync(out_host, p_out, out_bytes, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
             (e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {

@@ -27,6 +27,9 @@ struct vcd_ctx {
     int batch_rc_scalar_warps, batch_tx_threads;
     cudaGraphExec_t batch_graph;
     unsigned char batch_key[512];   // kernel parameters + shape + grid capacity the graph was captured with
+    // copy-out overlapped with the inverse transform (created on first use)
+    cudaStream_t copy_stream;
+    cudaEvent_t chunk_ev[8];
 };
 
 // Kernel statistics, accumulated while profiling is enabled (vcg_profile_enable).
