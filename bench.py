@@ -46,6 +46,7 @@ def args_parse():
     p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched-region measurement")
     p.add_argument("--no-served", action="store_true", help="skip the config-5 served-decode measurement")
     p.add_argument("--no-dct", action="store_true", help="skip the config-3 DCT-forms measurement")
+    p.add_argument("--no-sweep", action="store_true", help="skip the config-2 target / LOD sweep")
     p.add_argument("--dct-size", type=int, default=1024, help="edge of the DCT-forms volume")
     p.add_argument("--dct-reps", type=int, default=3, help="timed calls per DCT form and direction (0: one call)")
     return p.parse_args()
@@ -330,6 +331,69 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             "speedup_vs_plain": batch_gbps / plain_gbps, "autotuned_shape": {"rc_scalar_warps": shape[0],
                                                                             "transform_threads": shape[1]},
             "bit_exact_sample": ok, "plain_sample": plain_sample}
+
+
+def _stage_table(stats, peak):
+    """Per-stage device ms, algorithmic GB/s and fraction of the measured HBM peak."""
+    out = {}
+    for k, v in stats.items():
+        gbps = (v["bytes_read"] + v["bytes_written"]) / max(1e-9, v["ms"] / 1e3) / 1e9
+        out[k] = {"ms": v["ms"], "launches": v["launches"], "GBps_algorithmic": gbps, "hbm_frac": gbps / peak}
+    return out
+
+
+def config2_sweep(dvol, dims, peak, targets=(10.0, 50.0, 100.0)):
+    """The 1024^3 volume encoded at each target (rate control included) and every
+    LOD of each archive decoded into device memory: device time, GB/s and
+    per-stage algorithmic GB/s with the fraction of the measured HBM peak;
+    archives and decoded LODs are checked against the reference's SHA-256
+    fixtures where they exist."""
+    import hashlib
+    import vc_gb300 as vc
+    nx, ny, nz = dims
+    res = {}
+    for t in targets:
+        vc.profile_enable(True)
+        vc.profile_read(reset=True)
+        s, data, q0 = vc.encode_device(dvol, dims, t)
+        assert s == 0, vc.last_error()
+        enc_ms = vc.last_call_ms()
+        enc_stages = _stage_table(vc.profile_read(reset=True), peak)
+        vc.profile_enable(False)
+        g = golden_case(nx, t)
+        row = {"q0": q0, "archive_bytes": len(data), "ratio_over_volume": nx * ny * nz / len(data),
+               "encode_ms_profiled": enc_ms, "encode_stages": enc_stages,
+               "archive_sha_matches_reference": (hashlib.sha256(data).hexdigest() == g["sha256"]) if g else None}
+        s, _, _ = vc.encode_device(dvol, dims, t)   # unprofiled timing
+        row["encode_GBps"] = nx * ny * nz / (vc.last_call_ms() / 1e3) / 1e9
+        a = vc.Archive(data)
+        assert a.make_resident() == 0
+        lods, lod_ok = [], []
+        for lod in range(8):
+            s, (lx, ly, lz) = a.lod_dims(lod)
+            if s:
+                break
+            buf = vc.DeviceBuffer(max(1, lx * ly * lz))
+            assert a.decode_lod_device(lod, buf) == 0
+            vc.profile_enable(True)
+            vc.profile_read(reset=True)
+            ms = []
+            for _ in range(3):
+                assert a.decode_lod_device(lod, buf) == 0
+                ms.append(vc.last_call_ms())
+            st = _stage_table(vc.profile_read(reset=True), peak)
+            vc.profile_enable(False)
+            m = statistics.median(ms)
+            lods.append({"lod": lod, "dims": [lx, ly, lz], "ms": m, "GBps": lx * ly * lz / (m / 1e3) / 1e9,
+                         "stages": {k: {"ms": v["ms"] / 3, "hbm_frac": v["hbm_frac"]} for k, v in st.items()}})
+            if g:
+                lod_ok.append(hashlib.sha256(buf.download(lx * ly * lz).tobytes()).hexdigest() == g["lod_sha256"][lod])
+            buf.free()
+        a.close()
+        row["decode_lods"] = lods
+        row["lods_match_reference"] = all(lod_ok) if g else None
+        res[f"t{int(t)}"] = row
+    return res
 
 
 def _equal_device(vc, a, b, nbytes, chunk=256 << 20):
@@ -737,6 +801,9 @@ def gb300_arm(args, dist):
         if lod0_ok is None:
             lod0_ok = bool(np.array_equal(out.download(nbytes), ref_out.ravel()))
 
+    sweep = None
+    if dist.rank == 0 and not args.no_sweep:
+        sweep = config2_sweep(dvol, dims, peak)
     # the other workloads (rank 0): release the headline buffers first
     batched = dct = served = None
     if dist.rank == 0 and not (args.no_batched and args.no_dct and args.no_served):
@@ -784,6 +851,8 @@ def gb300_arm(args, dist):
         line["served_regions"] = served
     if dct:
         line["dct_forms"] = dct
+    if sweep:
+        line["config2_sweep"] = sweep
     print(json.dumps(line), flush=True)
 
 

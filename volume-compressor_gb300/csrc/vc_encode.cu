@@ -147,6 +147,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     }
     CK(vcd_scratch(c, VCD_BUF_PYR, pyr_bytes + 16, &p), "pyramid");
     cudaEventRecord(c->ev[6], st);   // device work starts (input already on the device)
+    const bool prof = vcd_prof_on();
     {
         uint8_t *q = (uint8_t *)p;
         for (int l = 1; l < nlod; ++l) {
@@ -154,6 +155,12 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
             S.lvol[l] = q;
             q += nvox[l];
         }
+    }
+    if (prof && nlod > 1) {   // pyramid: every coarser voxel reads its (up to) 8 children
+        cudaEventRecord(c->ev[5], st);
+        cudaEventSynchronize(c->ev[5]);
+        vcd_prof_add("downsample", vcd_elapsed(c->ev[6], c->ev[5]), (uint64_t)(nlod - 1), nvox[0] + pyr_bytes - nvox[nlod - 1],
+                     pyr_bytes, pyr_bytes);
     }
     const uint64_t chunk = total_atoms < kChunk ? total_atoms : kChunk;
     CK(vcd_scratch(c, VCD_BUF_EENT, chunk * VCD_MAX_ENTRIES * 4 + 16, &p), "coefficient lists");
@@ -241,8 +248,14 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     P.len = S.len;
     P.dc = S.dc;
     P.lay = S.lay;
+    if (prof) cudaEventRecord(c->ev[4], st);
     launch_consume(P, st);
     launch_scan_u64(S.pos, total_atoms, head, S.pos + total_atoms, st);
+    if (prof) {   // lengths in, consumed bytes out, scanned in place
+        cudaEventRecord(c->ev[5], st);
+        cudaEventSynchronize(c->ev[5]);
+        vcd_prof_add("encode_place", vcd_elapsed(c->ev[4], c->ev[5]), 2, total_atoms * 12, total_atoms * 16, total_atoms);
+    }
     uint64_t *pos_h = (uint64_t *)malloc((total_atoms + 1) * 8);
     if (!pos_h) return 3;
     cudaError_t e = cudaMemcpyAsync(pos_h, S.pos, (total_atoms + 1) * 8, cudaMemcpyDeviceToHost, st);
@@ -257,7 +270,13 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     P.arc = S.arc;
     cudaMemsetAsync(S.arc, 0, total, st);
     run_range(S, 0, total_atoms, true);
+    if (prof) cudaEventRecord(c->ev[4], st);
     launch_slots(P, st);
+    if (prof) {   // one 16-byte slot per atom
+        cudaEventRecord(c->ev[5], st);
+        cudaEventSynchronize(c->ev[5]);
+        vcd_prof_add("encode_slots", vcd_elapsed(c->ev[4], c->ev[5]), 1, total_atoms * 21, total_atoms * 16, total_atoms);
+    }
     cudaEventRecord(c->ev[7], st);   // device work ends (the archive head and copy-out follow)
 
     uint8_t *hd = (uint8_t *)calloc(head, 1);
