@@ -305,6 +305,20 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             ms.append(vc.last_call_ms())
     shape = vc.batch_shape()
     batch_ms = min(ms)
+    # every candidate of the autotuner on the same batch (forced shape, graph re-captured)
+    cand = {}
+    L = vc.lib()
+    for rcw in (1, 4, 16):
+        for tx, imma in ((256, 0), (512, 0), (256, 1)):
+            assert L.vcg_set_batch_shape(rcw, tx, imma) == 0
+            t = []
+            for k in range(3):
+                s, st = a.decode_regions(reqs, views, on_device=True)
+                assert s == 0 and (st == 0).all()
+                if k:
+                    t.append(vc.last_call_ms())
+            cand[f"rc{rcw}_{'imma' if imma else 'butterfly'}{tx}"] = min(t)
+    assert L.vcg_set_batch_shape(0, 0, 0) == 0
     # plain path: one vcg_decode_region_device per request, on a sample
     idx = rng.choice(n_boxes, plain_sample, replace=False)
     plain_ms, plain_bytes = [], 0
@@ -328,7 +342,7 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             "batched_ms": batch_ms, "batched_GBps": batch_gbps, "batched_us_per_request": batch_ms * 1e3 / n_boxes,
             "plain_GBps": plain_gbps, "plain_p50_us": plain_ms[len(plain_ms) // 2] * 1e3,
             "plain_p99_us": plain_ms[min(len(plain_ms) - 1, int(0.99 * len(plain_ms)))] * 1e3,
-            "speedup_vs_plain": batch_gbps / plain_gbps, "autotuned_shape": {"rc_scalar_warps": shape[0],
+            "speedup_vs_plain": batch_gbps / plain_gbps, "candidates_ms": cand, "autotuned_shape": {"rc_scalar_warps": shape[0], "transform_imma": shape[2],
                                                                             "transform_threads": shape[1]},
             "bit_exact_sample": ok, "plain_sample": plain_sample}
 

@@ -36,9 +36,16 @@ vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_request
                              vc_status *status);
 // Launch shape the calling thread uses (0 before its first batch): range-decoder
 // policy (warps per SM sub-partition that decode one atom each before atoms
-// share warps in lockstep; see vcg_set_rc_scalar_warps) and transform CTA size
-// (32 x warps per atom).
-void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads);
+// share warps in lockstep; see vcg_set_rc_scalar_warps), transform CTA size
+// (32 x warps per atom) and transform form (0 butterfly on the CUDA cores,
+// 1 int8 tensor cores). The autotuner times every combination on the process's
+// first batch; all give identical bytes.
+void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads, int *transform_imma);
+// Fix the shape of every later batch instead of autotuning (rc_scalar_warps 1,
+// 4 or 16; transform_threads 256 or 512 for the butterfly, 256 for the tensor
+// cores); rc_scalar_warps = 0 returns to the tuned shape. VC_ERR_RANGE for a
+// shape that is not a candidate.
+vc_status vcg_set_batch_shape(int rc_scalar_warps, int transform_threads, int transform_imma);
 
 // Range-decoder policy of vc_decode_region / vc_decode_lod / vc_decode_atom and
 // the device-output variants (process-wide; results do not depend on it). A

@@ -52,8 +52,8 @@ def test_batch_matches_plain_host_and_device(vc, gpu, golden, name):
     nlod = struct.unpack_from("<I", load_archive(golden[name]), 20)[0]
     check(vc, a, random_requests(a, rng, 60, min(nlod - 1, 3), invalid=3), on_device=False)
     check(vc, a, random_requests(a, rng, 60, min(nlod - 1, 3), invalid=2), on_device=True)
-    rc, tx = vc.batch_shape()
-    assert rc in (1, 4, 16) and tx in (256, 512)
+    rc, tx, imma = vc.batch_shape()
+    assert rc in (1, 4, 16) and tx in (256, 512) and imma in (0, 1)
 
 
 def test_batch_graph_replay_and_growth(vc, gpu, golden):
@@ -73,3 +73,28 @@ def test_batch_on_corrupt_archive_matches_plain(vc, gpu, golden):
     reqs = random_requests(a, rng, 40, 1, max_edge=97) + [(0, (0, 0, 0, 97, 131, 65))]
     check(vc, a, reqs, on_device=False)
     check(vc, a, reqs, on_device=True)
+
+
+@pytest.mark.parametrize("shape", [(1, 256, 0), (4, 256, 0), (16, 256, 0), (1, 512, 0), (4, 512, 0), (16, 512, 0),
+                                   (1, 256, 1), (4, 256, 1), (16, 256, 1)])
+def test_every_launch_shape_matches_plain(vc, gpu, golden, shape):
+    """Each candidate of the autotuner (range-decoder policy x transform size x
+    butterfly / int8 tensor-core transform) gives the plain decode's bytes and
+    statuses, also on a corrupt archive."""
+    from test_gpu_decode import _slot_offset
+    L = vc.lib()
+    assert L.vcg_set_batch_shape(*shape) == 0
+    try:
+        a = vc.Archive(load_archive(golden["synth_prime_97x131x65_t20"]))
+        rng = np.random.default_rng(14)
+        check(vc, a, random_requests(a, rng, 40, 2, max_edge=97, invalid=1), on_device=False)
+        assert vc.batch_shape() == shape
+        data = bytearray(load_archive(golden["synth_prime_97x131x65_t20"]))
+        so = _slot_offset(data, 0, 1, 2, 1)
+        struct.pack_into("<I", data, so + 8, len(data))
+        b = vc.Archive(bytes(data))
+        check(vc, b, random_requests(b, rng, 30, 1, max_edge=97) + [(0, (0, 0, 0, 97, 131, 65))], on_device=True)
+    finally:
+        assert L.vcg_set_batch_shape(0, 0, 0) == 0
+    assert L.vcg_set_batch_shape(2, 256, 0) == vc.VC_ERR_RANGE
+    assert L.vcg_set_batch_shape(4, 512, 1) == vc.VC_ERR_RANGE

@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include "idct_tile.cuh"
+#include "imma.cuh"
 #include "kernels.cuh"
 #include "rangecoder.cuh"
 
@@ -64,13 +65,55 @@ __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
     }
 }
 
+// window of box request r inside atom origin (gx, gy, gz), and its first voxel
+struct BoxWin {
+    Crop k;
+    uint64_t ox, oy;
+    uint8_t *ob;
+    __device__ __forceinline__ BoxWin(const BoxReq &r, uint32_t gx, uint32_t gy, uint32_t gz) {
+        k.set(gx, gy, gz, r.x0, r.y0, r.z0, r.x1, r.y1, r.z1);
+        ox = r.x1 - r.x0;
+        oy = r.y1 - r.y0;
+        ob = r.out + ((uint64_t)(gz + k.lz0 - r.z0) * oy + (gy + k.ly0 - r.y0)) * ox + (gx + k.lx0 - r.x0);
+    }
+};
+
+// ABSENT / KNOWN_ZERO / malformed atom: zeros in every box it overlaps
+template <int NT>
+__device__ __forceinline__ void zero_all(const BatchJob &J, const UAtom &a) {
+    for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) {
+        const BoxWin w(J.reqs[J.dst[d]], a.ax * 32, a.ay * 32, a.az * 32);
+        zero_window<NT>(w.ob, w.ox, w.oy, w.k);
+    }
+}
+
+// Butterfly inverse transform of distinct atom u (T: 128 KiB of shared memory),
+// cropped into every box it overlaps. Ends with a barrier.
+template <int NT>
+__device__ __forceinline__ void bf_atom_to_boxes(int32_t *T, const BatchJob &J, const UAtom &a, uint32_t u,
+                                                 const vcd_atom &e, uint32_t c, const int32_t *dqs,
+                                                 const int32_t *dqb, const uint32_t *alt) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int32_t dc = J.arc[e.off];
+    idct_tile_xy<NT>(T, J.arc, e, c, J.ent + J.ent_off[u], J.scan, J.band_start, dqs, dqb, alt);
+    for (int y = warp; y < 32; y += NT / 32) {
+        int32_t o[32];
+        idct_col_z(T, y, lane, o);
+        for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) {
+            const BoxWin w(J.reqs[J.dst[d]], a.ax * 32, a.ay * 32, a.az * 32);
+            store_col(w.ob, w.ox, w.oy, w.k, y, lane, o, dc);
+        }
+    }
+    __syncthreads();
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT, 1) k_idct_batch(BatchJob J) {
     extern __shared__ int32_t T[];
     __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
     __shared__ uint32_t alt[1024];
     __shared__ uint32_t s_u;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     for (int i = tid; i < 1024; i += NT) alt[i] = J.alt_mask[i];
     const uint32_t n = *J.n_ua;
     int cur_lod = -1;
@@ -88,33 +131,105 @@ __global__ void __launch_bounds__(NT, 1) k_idct_batch(BatchJob J) {
         }
         const vcd_atom e = J.atoms[a.idx];
         const uint32_t c = e.kind == VCD_PRESENT ? J.cnt[u] : kEntBad;
-        const uint32_t gx = a.ax * 32, gy = a.ay * 32, gz = a.az * 32;
         if (e.kind != VCD_PRESENT || (c & kEntBad)) {   // ABSENT / KNOWN_ZERO -> zeros in every box
-            for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) {
-                const BoxReq r = J.reqs[J.dst[d]];
-                Crop k;
-                k.set(gx, gy, gz, r.x0, r.y0, r.z0, r.x1, r.y1, r.z1);
-                const uint64_t ox = r.x1 - r.x0, oy = r.y1 - r.y0;
-                uint8_t *ob = r.out + ((uint64_t)(gz + k.lz0 - r.z0) * oy + (gy + k.ly0 - r.y0)) * ox + (gx + k.lx0 - r.x0);
-                zero_window<NT>(ob, ox, oy, k);
-            }
+            zero_all<NT>(J, a);
             continue;
         }
-        const int32_t dc = J.arc[e.off];
-        idct_tile_xy<NT>(T, J.arc, e, c, J.ent + J.ent_off[u], J.scan, J.band_start, dqs, dqb, alt);
-        for (int y = warp; y < 32; y += NT / 32) {
-            int32_t o[32];
-            idct_col_z(T, y, lane, o);
-            for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) {
-                const BoxReq r = J.reqs[J.dst[d]];
-                Crop k;
-                k.set(gx, gy, gz, r.x0, r.y0, r.z0, r.x1, r.y1, r.z1);
-                const uint64_t ox = r.x1 - r.x0, oy = r.y1 - r.y0;
-                uint8_t *ob = r.out + ((uint64_t)(gz + k.lz0 - r.z0) * oy + (gy + k.ly0 - r.y0)) * ox + (gx + k.lx0 - r.x0);
-                store_col(ob, ox, oy, k, y, lane, o, dc);
-            }
+        bf_atom_to_boxes<NT>(T, J, a, u, e, c, dqs, dqb, alt);
+    }
+}
+
+// The same on the int8 tensor cores: the nonzero levels are dequantised and
+// scattered as three int8 pieces into piece planes (imma.cuh), the three
+// inverse passes run as MMAs, the voxels are staged in shared memory and
+// cropped into every box. Lists that overflowed their capacity and atoms whose
+// values leave the three-piece range take the butterfly, so every result is
+// the reference's.
+constexpr size_t kImmaSmem = 2 * 3 * 32768;   // two buffers of three piece planes
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_idct_batch_imma(BatchJob J) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
+    __shared__ uint32_t alt[1024];
+    __shared__ uint32_t s_u;
+    __shared__ int s_bad;
+    const int tid = threadIdx.x;
+    uint32_t A[2][2][4];
+    imma_a_frags<true>(A);
+    for (int i = tid; i < 1024; i += NT) alt[i] = J.alt_mask[i];
+    const uint32_t n = *J.n_ua;
+    int cur_lod = -1;
+    for (;;) {
+        if (tid == 0) {
+            s_u = atomicAdd(J.work, 1u);
+            s_bad = 0;
         }
         __syncthreads();
+        const uint32_t u = s_u;
+        __syncthreads();
+        if (u >= n) break;
+        const UAtom a = J.ua[u];
+        if ((int)a.lod != cur_lod) {   // uniform: dequantisation tables of this LOD
+            for (int i = tid; i < VCD_NCLASS; i += NT) { dqs[i] = J.dq[a.lod].step[i]; dqb[i] = J.dq[a.lod].bias[i]; }
+            cur_lod = (int)a.lod;
+            __syncthreads();
+        }
+        const vcd_atom e = J.atoms[a.idx];
+        const uint32_t c = e.kind == VCD_PRESENT ? J.cnt[u] : kEntBad;
+        if (e.kind != VCD_PRESENT || (c & kEntBad)) {
+            zero_all<NT>(J, a);
+            continue;
+        }
+        if (!(c & kEntOverflow)) {
+            int4 *P4 = reinterpret_cast<int4 *>(sm);
+            for (int i = tid; i < 3 * 32768 / 16; i += NT) P4[i] = make_int4(0, 0, 0, 0);
+            __syncthreads();
+            bool bad = false;
+            const uint32_t cnt = c & kEntMask;
+            const uint32_t *src = J.ent + J.ent_off[u];
+            for (uint32_t i = tid; i < cnt; i += NT) {
+                const uint32_t w = src[i];
+                const uint32_t r = __ldg(J.scan + (w & 0xFFFFu));
+                const int32_t v = dequant((int16_t)(w >> 16), r, dqs, dqb, alt);
+                bad |= !fits<3>(v);
+                const int off = (int)(r >> 5) * 32 + ppos((int)(r & 31u));   // line (kz, ky), element kx
+#pragma unroll
+                for (int j = 0; j < 3; ++j) imma_plane<3>(sm, 0, j)[off] = (uint8_t)piece<3>(v, j);
+            }
+            if (bad) s_bad = 1;
+            __syncthreads();
+            if (!s_bad) {
+                const int32_t dc = J.arc[e.off];
+                uint8_t *vox = imma_plane<3>(sm, 1, 0);   // free while the last pass reads buffer 0
+#pragma unroll 1
+                for (int pass = 0; pass < 3; ++pass) {
+                    imma_pass<3, NT>(sm, A, pass, bad, [&](int k, int la, int lb, int32_t o0, int32_t o1) {
+                        const int32_t v0 = o0 + dc, v1 = o1 + dc;
+                        const uint32_t b0 = (uint32_t)(v0 < 0 ? 0 : (v0 > 255 ? 255 : v0));
+                        const uint32_t b1 = (uint32_t)(v1 < 0 ? 0 : (v1 > 255 ? 255 : v1));
+                        *reinterpret_cast<uint16_t *>(vox + k * 1024 + la * 32 + lb) = (uint16_t)(b0 | (b1 << 8));
+                    });
+                    if (bad) s_bad = 1;
+                    __syncthreads();
+                }
+                if (!s_bad) {   // voxels (z, y, x) of the atom -> every box it overlaps
+                    for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) {
+                        const BoxWin w(J.reqs[J.dst[d]], a.ax * 32, a.ay * 32, a.az * 32);
+                        const uint32_t cw = w.k.lx1 - w.k.lx0, ch = w.k.ly1 - w.k.ly0, cd = w.k.lz1 - w.k.lz0;
+                        for (uint32_t i = tid; i < ch * cd; i += NT) {
+                            const uint32_t y = i % ch, z = i / ch;
+                            const uint8_t *sr = vox + (w.k.lz0 + z) * 1024 + (w.k.ly0 + y) * 32 + w.k.lx0;
+                            uint8_t *dr = w.ob + ((uint64_t)z * w.oy + y) * w.ox;
+                            for (uint32_t x = 0; x < cw; ++x) dr[x] = sr[x];
+                        }
+                    }
+                    __syncthreads();
+                    continue;
+                }
+            }
+        }
+        bf_atom_to_boxes<NT>(reinterpret_cast<int32_t *>(sm), J, a, u, e, c, dqs, dqb, alt);
     }
 }
 
@@ -149,8 +264,18 @@ void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint3
     Jr.rc_scalar_warps = (uint32_t)shape.rc_scalar_warps;
     Jr.sms = (uint32_t)num_sms;
     launch_rc(Jr, num_sms, max_ua, s);
-    if (shape.idct_threads == 512) launch_tx<512>(J, num_sms, s);
-    else launch_tx<256>(J, num_sms, s);
+    if (shape.imma) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_idct_batch_imma<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kImmaSmem);
+            attr = true;
+        }
+        k_idct_batch_imma<256><<<num_sms, 256, kImmaSmem, s>>>(J);
+    } else if (shape.idct_threads == 512) {
+        launch_tx<512>(J, num_sms, s);
+    } else {
+        launch_tx<256>(J, num_sms, s);
+    }
 }
 
 }  // namespace vcg

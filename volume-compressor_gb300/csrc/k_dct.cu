@@ -32,6 +32,7 @@
 
 #include "../../include/vcg.h"
 #include "dct32.cuh"
+#include "imma.cuh"
 #include "vc_device.h"
 
 namespace vcg {
@@ -179,57 +180,14 @@ __global__ void __launch_bounds__(kDctThreads, 1) k_dct_bf(DctJob J) {
 }
 
 // ------------------------------------------------------------------ imma
-__constant__ int32_t c_cmat[32][32] = VC_CMAT_INIT;
-
-// Byte of element n in a 32-byte piece line, arranged so that lane (g, t) of
-// an m16n8k32 B fragment finds its elements n = 4t..4t+3 and 16+4t..16+4t+3 as
-// one aligned 8-byte word.
-__device__ __forceinline__ int ppos(int n) { return (((n & 15) >> 2) << 3) | ((n >> 4) << 2) | (n & 3); }
-
-__device__ __forceinline__ void mma_s8(int32_t (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-        : "+r"(d[0]), "+r"(d[1]), "+r"(d[2]), "+r"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// piece j of v (VP pieces): low pieces 7 bits, the top piece signed
-template <int VP>
-__device__ __forceinline__ uint32_t piece(int32_t v, int j) {
-    return j < VP - 1 ? (uint32_t)(v >> (7 * j)) & 127u : (uint32_t)(v >> (7 * (VP - 1))) & 0xFFu;
-}
-template <int VP>
-__device__ __forceinline__ bool fits(int32_t v) {
-    const int32_t top = v >> (7 * (VP - 1));
-    return top >= -128 && top <= 127;
-}
-
 template <bool INV, int VP>
 __global__ void __launch_bounds__(kDctThreads, 1) k_dct_imma(DctJob J) {
     extern __shared__ __align__(16) uint8_t sm[];
     __shared__ int s_bad;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g = lane >> 2, t = lane & 3;
-    // A fragments of the two coefficient pieces: rows g, g+8 (+16 per m-tile),
-    // columns 4t..4t+3 and 16+4t..16+4t+3; A = C (forward) or C^T (inverse)
+    const int tid = threadIdx.x;
     uint32_t A[2][2][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int cp = 0; cp < 2; ++cp)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const int row = mt * 16 + g + (r & 1) * 8, col0 = (r >> 1) * 16 + t * 4;
-                uint32_t w = 0;
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const int32_t c = INV ? c_cmat[col0 + b][row] : c_cmat[row][col0 + b];
-                    const uint32_t p = cp ? (uint32_t)(c >> 7) & 0xFFu : (uint32_t)c & 127u;
-                    w |= p << (8 * b);
-                }
-                A[mt][cp][r] = w;
-            }
-    // piece plane j of ping-pong buffer b
-    auto plane = [&](int b, int j) -> uint8_t * { return sm + (b * VP + j) * 32768; };
+    imma_a_frags<INV>(A);
+    auto plane = [&](int b, int j) -> uint8_t * { return imma_plane<VP>(sm, b, j); };
 
     for (uint64_t a = blockIdx.x; a < J.n_atoms; a += gridDim.x) {
         uint64_t bx, by, bz;
@@ -286,64 +244,15 @@ __global__ void __launch_bounds__(kDctThreads, 1) k_dct_imma(DctJob J) {
 
 #pragma unroll 1
         for (int pass = 0; pass < 3; ++pass) {
-            const int sb = pass & 1, db = sb ^ 1;
-#pragma unroll 1
-            for (int tile = warp; tile < 128; tile += kDctThreads / 32) {
-                const int L0 = tile * 8;
-                uint32_t B[VP][2];
-#pragma unroll
-                for (int j = 0; j < VP; ++j) {
-                    const uint2 w = *reinterpret_cast<const uint2 *>(plane(sb, j) + (L0 + g) * 32 + t * 8);
-                    B[j][0] = w.x;
-                    B[j][1] = w.y;
+            imma_pass<VP, kDctThreads>(sm, A, pass, bad, [&](int k, int la, int lb, int32_t o0, int32_t o1) {
+                if (!INV) {
+                    *reinterpret_cast<int2 *>(J.coef_out + a * 32768 + (k * 32 + la) * 32 + lb) = make_int2(o0, o1);
+                } else {
+                    const uint32_t v2 = (uint32_t)clamp_u8(o0 + cen) | ((uint32_t)clamp_u8(o1 + cen) << 8);
+                    *reinterpret_cast<uint16_t *>(J.vol_out + ((bz + k) * J.ny + by + la) * J.nx + bx + lb) =
+                        (uint16_t)v2;
                 }
-                int32_t acc[2][VP + 1][4];
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                    for (int w = 0; w <= VP; ++w)
-#pragma unroll
-                        for (int r = 0; r < 4; ++r) acc[mt][w][r] = 0;
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                    for (int cp = 0; cp < 2; ++cp)
-#pragma unroll
-                        for (int j = 0; j < VP; ++j) mma_s8(acc[mt][cp + j], A[mt][cp], B[j][0], B[j][1]);
-                // epilogue: lane holds rows k = 16 mt + 8 h + g of lines L0 + 2t, L0 + 2t + 1
-                const int line = L0 + 2 * t, la = line >> 5, lb = line & 31;
-#pragma unroll
-                for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int k = mt * 16 + h * 8 + g;
-                        int32_t o[2];
-#pragma unroll
-                        for (int e = 0; e < 2; ++e) {
-                            uint32_t s = 0;
-#pragma unroll
-                            for (int w = 0; w <= VP; ++w) s += (uint32_t)acc[mt][w][h * 2 + e] << (7 * w);
-                            o[e] = (int32_t)(s + 8192u) >> 14;
-                        }
-                        if (pass < 2) {
-                            // rotate (a, b, k) -> line' = k*32 + a, element b
-                            bad |= !fits<VP>(o[0]) || !fits<VP>(o[1]);
-                            const int off = (k * 32 + la) * 32 + ppos(lb);
-#pragma unroll
-                            for (int j = 0; j < VP; ++j)
-                                *reinterpret_cast<uint16_t *>(plane(db, j) + off) =
-                                    (uint16_t)(piece<VP>(o[0], j) | (piece<VP>(o[1], j) << 8));
-                        } else if (!INV) {
-                            *reinterpret_cast<int2 *>(J.coef_out + a * 32768 + (k * 32 + la) * 32 + lb) =
-                                make_int2(o[0], o[1]);
-                        } else {
-                            const uint32_t v2 = (uint32_t)clamp_u8(o[0] + cen) |
-                                                ((uint32_t)clamp_u8(o[1] + cen) << 8);
-                            *reinterpret_cast<uint16_t *>(J.vol_out + ((bz + k) * J.ny + by + la) * J.nx + bx + lb) =
-                                (uint16_t)v2;
-                        }
-                    }
-            }
+            });
             if (bad) s_bad = 1;
             __syncthreads();
         }

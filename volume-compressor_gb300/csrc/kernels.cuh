@@ -72,6 +72,7 @@ struct BatchJob {
 struct BatchShape {              // tunables the autotuner chooses among
     int rc_scalar_warps;         // range-decoder policy: 1, 4 or 16 (rc_lanes_for)
     int idct_threads;            // transform CTA size (warps per atom x 32): 256 or 512
+    int imma;                    // transform on the int8 tensor cores (256 threads) instead of the butterfly
 };
 
 // Atoms per warp for the range decoder. A warp that decodes one atom runs the

@@ -3,7 +3,8 @@
 // grow-only device buffers, then replay one CUDA graph of the persistent
 // range-decode + transform launches. The launch shape (range-decoder policy:
 // warps per SM sub-partition that decode one atom each before atoms share warps
-// in lockstep; transform CTA size = 32 x warps per atom) is picked once per process by timing every candidate on
+// in lockstep; transform on the CUDA cores with 8 or 16 warps per atom, or on
+// the int8 tensor cores) is picked once per process by timing every candidate on
 // the first batch (all candidates produce identical bytes); threads that start
 // later take the tuned shape.
 #include <cuda_runtime.h>
@@ -19,7 +20,8 @@ using namespace vcg;
 
 #define VC_API extern "C" __attribute__((visibility("default")))
 
-static const BatchShape kShapes[] = {{1, 256}, {4, 256}, {16, 256}, {1, 512}, {4, 512}, {16, 512}};
+static const BatchShape kShapes[] = {{1, 256, 0}, {4, 256, 0}, {16, 256, 0}, {1, 512, 0}, {4, 512, 0},
+                                     {16, 512, 0}, {1, 256, 1}, {4, 256, 1}, {16, 256, 1}};
 
 #define CKB(call, what)                                \
     do {                                               \
@@ -32,8 +34,10 @@ static const BatchShape kShapes[] = {{1, 256}, {4, 256}, {16, 256}, {1, 512}, {4
 
 static size_t cap_of(const vcd_ctx *c, int slot) { return c->cap[slot]; }
 
-// tuned shape shared by all threads: rc_threads << 16 | transform threads (0 = not yet)
+// tuned shape shared by all threads: rc policy << 20 | imma << 16 | transform threads (0 = not yet)
 static int g_tuned_shape = 0;
+// shape set by vcg_set_batch_shape, same packing (0 = autotune)
+static int g_forced_shape = 0;
 
 extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *const *host_out, uint32_t *req_err) {
     vcd_ctx *c = vcd_thread_ctx();
@@ -90,9 +94,23 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
     // capacity in distinct atoms the range-decode grid must cover (the buffer's)
     const uint32_t max_ua = (uint32_t)((cap_of(c, VCD_BUF_BUA) - 64) / sizeof(vcd_uatom));
 
+    const int forced = __atomic_load_n(&g_forced_shape, __ATOMIC_ACQUIRE);
+    if (forced) {
+        c->batch_rc_scalar_warps = forced >> 20;
+        c->batch_imma = (forced >> 16) & 1;
+        c->batch_tx_threads = forced & 0xFFFF;
+        c->batch_forced = 1;
+    } else if (c->batch_forced) {   // back to the tuned shape
+        c->batch_rc_scalar_warps = 0;
+        c->batch_forced = 0;
+    }
     if (!c->batch_rc_scalar_warps) {
         const int t = __atomic_load_n(&g_tuned_shape, __ATOMIC_ACQUIRE);
-        if (t) { c->batch_rc_scalar_warps = t >> 16; c->batch_tx_threads = t & 0xFFFF; }
+        if (t) {
+            c->batch_rc_scalar_warps = t >> 20;
+            c->batch_imma = (t >> 16) & 1;
+            c->batch_tx_threads = t & 0xFFFF;
+        }
     }
     if (!c->batch_rc_scalar_warps) {   // autotune on the process's first batch
         float best = 1e30f;
@@ -104,13 +122,19 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
             CKB(cudaEventSynchronize(c->ev[1]), "autotune");
             CKB(cudaGetLastError(), "autotune");
             float ms = vcd_elapsed(c->ev[0], c->ev[1]);
-            if (ms < best) { best = ms; c->batch_rc_scalar_warps = s.rc_scalar_warps; c->batch_tx_threads = s.idct_threads; }
+            if (ms < best) {
+                best = ms;
+                c->batch_rc_scalar_warps = s.rc_scalar_warps;
+                c->batch_tx_threads = s.idct_threads;
+                c->batch_imma = s.imma;
+            }
         }
         CKB(cudaMemsetAsync(ctl + 1, 0, 4, st), "reset");
         CKB(cudaMemsetAsync(ctl + 4, 0, (size_t)b->n_req * 4, st), "reset");
-        __atomic_store_n(&g_tuned_shape, c->batch_rc_scalar_warps << 16 | c->batch_tx_threads, __ATOMIC_RELEASE);
+        __atomic_store_n(&g_tuned_shape, c->batch_rc_scalar_warps << 20 | c->batch_imma << 16 | c->batch_tx_threads,
+                         __ATOMIC_RELEASE);
     }
-    const BatchShape shape = {c->batch_rc_scalar_warps, c->batch_tx_threads};
+    const BatchShape shape = {c->batch_rc_scalar_warps, c->batch_tx_threads, c->batch_imma};
     // the graph bakes in every kernel parameter (buffers, archive tables) and the
     // grid size: replay it only when all of them are unchanged
     unsigned char key[512];
@@ -162,9 +186,29 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
     return 0;
 }
 
+// Fix the launch shape of every later batch (rc_scalar_warps 1, 4 or 16;
+// transform_threads 256 or 512 for the butterfly, 256 for the tensor cores);
+// rc_scalar_warps = 0 returns to the autotuned shape. Results do not depend on it.
+VC_API int vcg_set_batch_shape(int rc_scalar_warps, int transform_threads, int transform_imma) {
+    if (rc_scalar_warps == 0) {
+        __atomic_store_n(&g_forced_shape, 0, __ATOMIC_RELEASE);
+        return 0;
+    }
+    for (const BatchShape &s : kShapes) {
+        if (s.rc_scalar_warps == rc_scalar_warps && s.idct_threads == transform_threads &&
+            s.imma == (transform_imma ? 1 : 0)) {
+            __atomic_store_n(&g_forced_shape, rc_scalar_warps << 20 | s.imma << 16 | transform_threads,
+                             __ATOMIC_RELEASE);
+            return 0;
+        }
+    }
+    return 2;   // VC_ERR_RANGE
+}
+
 // Launch shape the calling thread uses (0 before its first batch).
-VC_API void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads) {
+VC_API void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads, int *transform_imma) {
     vcd_ctx *c = vcd_thread_ctx();
     if (rc_scalar_warps) *rc_scalar_warps = c ? c->batch_rc_scalar_warps : 0;
     if (transform_threads) *transform_threads = c ? c->batch_tx_threads : 0;
+    if (transform_imma) *transform_imma = c ? c->batch_imma : 0;
 }

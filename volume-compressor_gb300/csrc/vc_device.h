@@ -24,7 +24,7 @@ struct vcd_ctx {
     cudaEvent_t ev[8];           // stage events of the last call on this thread
     double last_ms;              // device time of the last decode / encode call (start..end events)
     // batched decode: autotuned launch shape and the CUDA graph of its launches
-    int batch_rc_scalar_warps, batch_tx_threads;
+    int batch_rc_scalar_warps, batch_tx_threads, batch_imma, batch_forced;
     cudaGraphExec_t batch_graph;
     unsigned char batch_key[512];   // kernel parameters + shape + grid capacity the graph was captured with
     // copy-out overlapped with the inverse transform (created on first use)

@@ -22,7 +22,7 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
               "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_rc_scalar_warps", "vcg_dct_forward", "vcg_dct_inverse",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_set_rc_scalar_warps", "vcg_dct_forward", "vcg_dct_inverse",
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
@@ -106,9 +106,10 @@ def dct_inverse(coef, dims, centre, form, vol, dc=None):
 
 
 def batch_shape():
-    a, b = ctypes.c_int(), ctypes.c_int()
-    lib().vcg_batch_shape(ctypes.byref(a), ctypes.byref(b))
-    return a.value, b.value
+    """(range-decoder policy, transform threads, transform on the tensor cores) the autotuner chose."""
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib().vcg_batch_shape(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    return a.value, b.value, c.value
 
 
 P = ctypes.c_void_p
@@ -165,7 +166,8 @@ def lib():
         L.vcg_last_error.restype = ctypes.c_char_p
         L.vcg_decode_atoms_noalloc.argtypes = [P, ctypes.c_size_t, P, P, ctypes.c_uint32, ctypes.c_float, P]
         L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
-        L.vcg_batch_shape.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        L.vcg_batch_shape.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+        L.vcg_set_batch_shape.argtypes = [ctypes.c_int] * 3
         L.vcg_set_rc_scalar_warps.argtypes = [ctypes.c_int]
         L.vcg_dct_forward.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, P, ctypes.POINTER(ctypes.c_uint32)]
         L.vcg_dct_inverse.argtypes = [P, P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
