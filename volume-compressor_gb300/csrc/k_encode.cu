@@ -61,38 +61,79 @@ __device__ __forceinline__ void load_row(const uint8_t *vol, uint32_t nx, uint32
     for (uint32_t i = 0; i < cnt; ++i) w[i >> 2] |= (uint32_t)__ldg(p + i) << (8 * (i & 3));
 }
 
+// Dead-zone quantiser of coefficient cf at raster r, as the release build
+// evaluates it (src/vc/vc.c:293-306): step class from the frequency and the
+// alternate-step bit, level = trunc((|cf| - dz) r' + 1) for |cf| >= dz, clamped.
+__device__ __forceinline__ int32_t quant_level(int32_t cf, uint32_t r, const float *qdz, const float *qrr,
+                                               const uint32_t *alt) {
+    const uint32_t f = (r >> 10) + ((r >> 5) & 31u) + (r & 31u);
+    const uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
+    const uint32_t mag = cf < 0 ? 0u - (uint32_t)cf : (uint32_t)cf;
+    const float fa = __int2float_rn((int32_t)mag);
+    int32_t level = 0;
+    if (fa >= qdz[cls]) {
+        level = __float2int_rz(__fadd_rn(__fmul_rn(__fsub_rn(fa, qdz[cls]), qrr[cls]), 1.0f));
+        if (level > 32767) level = 32767;
+    }
+    return cf < 0 ? -level : level;
+}
+
+// Quantise one atom in scan order and compact its nonzero levels into the list
+// dst (scan position | level << 16, in scan order); returns the count (every
+// thread). Warp w owns scan positions [4096 w, 4096 w + 4096), 32 at a time, so
+// coefficient reads, level stores and list writes are contiguous per warp:
+// pass 1 quantises (coef(p, r) gives the coefficient of scan position p, raster
+// r), keeps the levels in lv and counts them with warp ballots; pass 2 writes
+// the entries at the warp's offset. NT must be 256.
+template <int NT, class Coef>
+__device__ __forceinline__ uint32_t quant_compact(Coef &&coef, const uint16_t *scan, const float *qdz,
+                                                  const float *qrr, const uint32_t *alt, int16_t *lv,
+                                                  uint32_t *wcnt, uint32_t *dst) {
+    static_assert(NT == 256, "eight warps of 4096 scan positions");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t p0 = (uint32_t)warp * 4096u;
+    uint32_t cnt = 0;
+#pragma unroll 4
+    for (uint32_t i = 0; i < 4096; i += 32) {
+        const uint32_t p = p0 + i + lane;
+        const uint32_t r = __ldg(scan + p);
+        const int32_t level = quant_level(coef(p, r), r, qdz, qrr, alt);
+        lv[p] = (int16_t)level;
+        cnt += __popc(__ballot_sync(0xFFFFFFFFu, level != 0));
+    }
+    if (lane == 0) wcnt[warp] = cnt;
+    __syncthreads();
+    uint32_t base = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) {
+        const uint32_t v = wcnt[w];
+        base += w < warp ? v : 0u;
+        total += v;
+    }
+    const uint32_t below = (1u << lane) - 1u;
+#pragma unroll 4
+    for (uint32_t i = 0; i < 4096; i += 32) {
+        const uint32_t p = p0 + i + lane;
+        const int32_t level = lv[p];
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, level != 0);
+        if (level) dst[base + __popc(m & below)] = p | ((uint32_t)(uint16_t)level << 16);
+        base += __popc(m);
+    }
+    __syncthreads();   // lv and wcnt are reused by the next atom
+    return total;
+}
+
 __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
     extern __shared__ int32_t smem[];
     int32_t *T = smem;                                          // 32 slabs x swizzled 32x32
     int16_t *L = reinterpret_cast<int16_t *>(smem + 32768);     // levels in scan order
     __shared__ float qdz[VCD_NCLASS], qrr[VCD_NCLASS];
-    __shared__ uint16_t rank[94 * 32];
     __shared__ uint32_t alt[1024];
     __shared__ uint32_t red[32];
-    __shared__ uint32_t scanbuf[kFwdThreads / 32];
+    __shared__ uint32_t wcnt[kFwdThreads / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < 94 * 32; i += kFwdThreads) rank[i] = J.rank_base[i];
     for (int i = tid; i < 1024; i += kFwdThreads) alt[i] = J.alt_mask[i];
     int cur_lod = -1;
-
-    // quantise coefficient cf at (kz, ky, kx = lane) and scatter its level to scan order
-    auto quant_scatter = [&](int32_t cf, int kz, int ky) {
-        const uint32_t f = (uint32_t)(kz + ky + lane);
-        const uint32_t r = (uint32_t)(kz * 1024 + ky * 32 + lane);
-        const uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
-        const uint32_t mag = cf < 0 ? 0u - (uint32_t)cf : (uint32_t)cf;
-        const float fa = __int2float_rn((int32_t)mag);
-        int32_t level = 0;
-        if (fa >= qdz[cls]) {
-            level = __float2int_rz(__fadd_rn(__fmul_rn(__fsub_rn(fa, qdz[cls]), qrr[cls]), 1.0f));
-            if (level > 32767) level = 32767;
-        }
-        if (level) {
-            int sub = (int)f - kz - 31;
-            uint32_t p = (uint32_t)rank[f * 32 + kz] + (uint32_t)ky - (uint32_t)(sub > 0 ? sub : 0);
-            L[p] = (int16_t)(cf < 0 ? -level : level);
-        }
-    };
 
     for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
         int lod;
@@ -106,8 +147,9 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
         }
         const bool cached = J.coef && ca < J.coef_n;
         int32_t *cptr = cached ? J.coef + ca * 32768ull : nullptr;
-        int4 *L4 = reinterpret_cast<int4 *>(L);
+        uint32_t *dst = J.ent + t * (uint64_t)VCD_MAX_ENTRIES;
         int32_t dc;
+        uint32_t total;
         if (cached && !J.coef_store) {
             // the transform of this atom was kept: quantise straight from it
             const uint32_t dcz = J.coef_dc[ca];
@@ -116,129 +158,108 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
                 continue;
             }
             dc = (int32_t)(dcz & 0xFFu);
-            for (int i = tid; i < 32768 * 2 / 16; i += kFwdThreads) L4[i] = make_int4(0, 0, 0, 0);
-            __syncthreads();
-            for (int ky = warp; ky < 32; ky += kFwdThreads / 32) {
-                int32_t o[32];
-#pragma unroll
-                for (int kz = 0; kz < 32; ++kz) o[kz] = __ldcs(cptr + kz * 1024 + ky * 32 + lane);
-#pragma unroll
-                for (int kz = 0; kz < 32; ++kz) quant_scatter(o[kz], kz, ky);
-            }
-            __syncthreads();
+            total = quant_compact<kFwdThreads>([&](uint32_t p, uint32_t) { return __ldcs(cptr + p); }, J.scan, qdz,
+                                               qrr, alt, L, wcnt, dst);
         } else {
-        const uint8_t *vol = J.vol[lod];
-        const uint32_t nx = J.dims[lod][0], ny = J.dims[lod][1], nz = J.dims[lod][2];
-        // rows r = tid + 256 j: z = r >> 5, y = r & 31 (lane)
-        uint32_t w[4][8];
-        uint32_t s = 0;
+            const uint8_t *vol = J.vol[lod];
+            const uint32_t nx = J.dims[lod][0], ny = J.dims[lod][1], nz = J.dims[lod][2];
+            // rows r = tid + 256 j: z = r >> 5, y = r & 31 (lane)
+            uint32_t w[4][8];
+            uint32_t s = 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            int r = tid + kFwdThreads * j;
-            load_row(vol, nx, ny, nz, ax * 32, ay * 32 + (r & 31), az * 32 + (r >> 5), w[j]);
+            for (int j = 0; j < 4; ++j) {
+                int r = tid + kFwdThreads * j;
+                load_row(vol, nx, ny, nz, ax * 32, ay * 32 + (r & 31), az * 32 + (r >> 5), w[j]);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) s = __dp4a(w[j][i], 0x01010101u, s);
-        }
-        // zero the scan-order level buffer while the sum reduces
-        for (int i = tid; i < 32768 * 2 / 16; i += kFwdThreads) L4[i] = make_int4(0, 0, 0, 0);
+                for (int i = 0; i < 8; ++i) s = __dp4a(w[j][i], 0x01010101u, s);
+            }
 #pragma unroll
-        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
-        if (lane == 0) red[warp] = s;
-        __syncthreads();
-        uint32_t sum = 0;
+            for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+            if (lane == 0) red[warp] = s;
+            __syncthreads();
+            uint32_t sum = 0;
 #pragma unroll
-        for (int i = 0; i < kFwdThreads / 32; ++i) sum += red[i];
-        if (sum == 0) {   // all-zero atom: no payload (src/vc/vc.c:601)
-            if (tid == 0) {
-                J.meta[t] = kMetaZero;
-                if (cached) J.coef_dc[ca] = kMetaZero;
+            for (int i = 0; i < kFwdThreads / 32; ++i) sum += red[i];
+            if (sum == 0) {   // all-zero atom: no payload (src/vc/vc.c:601)
+                if (tid == 0) {
+                    J.meta[t] = kMetaZero;
+                    if (cached) J.coef_dc[ca] = kMetaZero;
+                }
+                __syncthreads();
+                continue;
+            }
+            dc = (int32_t)((sum + 16384u) / 32768u);
+            if (cached && tid == 0) J.coef_dc[ca] = (uint32_t)dc;
+            // pass along x for the thread's 4 rows, straight from registers
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int r = tid + kFwdThreads * j;
+                int32_t v[32], o[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) v[i] = (int32_t)((w[j][i >> 2] >> (8 * (i & 3))) & 0xFFu) - dc;
+                fdct32_line(v, o);
+                int32_t *S = T + (r >> 5) * 1024;
+#pragma unroll
+                for (int k = 0; k < 32; ++k) S[swz(r & 31, k)] = o[k];
             }
             __syncthreads();
-            continue;
-        }
-        dc = (int32_t)((sum + 16384u) / 32768u);
-        if (cached && tid == 0) J.coef_dc[ca] = (uint32_t)dc;
-        // pass along x for the thread's 4 rows, straight from registers
+            // pass along y, warp per z-slab, lane per column kx
+            for (int z = warp; z < 32; z += kFwdThreads / 32) {
+                int32_t *S = T + z * 1024;
+                int32_t v[32], o[32];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            int r = tid + kFwdThreads * j;
-            int32_t v[32], o[32];
+                for (int y = 0; y < 32; ++y) v[y] = S[swz(y, lane)];
+                fdct32_line(v, o);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] = (int32_t)((w[j][i >> 2] >> (8 * (i & 3))) & 0xFFu) - dc;
-            fdct32_line(v, o);
-            int32_t *S = T + (r >> 5) * 1024;
-#pragma unroll
-            for (int k = 0; k < 32; ++k) S[swz(r & 31, k)] = o[k];
-        }
-        __syncthreads();
-        // pass along y, warp per z-slab, lane per column kx
-        for (int z = warp; z < 32; z += kFwdThreads / 32) {
-            int32_t *S = T + z * 1024;
-            int32_t v[32], o[32];
-#pragma unroll
-            for (int y = 0; y < 32; ++y) v[y] = S[swz(y, lane)];
-            fdct32_line(v, o);
-#pragma unroll
-            for (int k = 0; k < 32; ++k) S[swz(k, lane)] = o[k];
-        }
-        __syncthreads();
-        // pass along z per column (ky, kx = lane), quantise, scatter to scan order
-        for (int ky = warp; ky < 32; ky += kFwdThreads / 32) {
-            int32_t v[32], o[32];
-#pragma unroll
-            for (int z = 0; z < 32; ++z) v[z] = T[z * 1024 + swz(ky, lane)];
-            fdct32_line(v, o);
-            if (cached) {
-#pragma unroll
-                for (int kz = 0; kz < 32; ++kz) cptr[kz * 1024 + ky * 32 + lane] = o[kz];
+                for (int k = 0; k < 32; ++k) S[swz(k, lane)] = o[k];
             }
+            __syncthreads();
+            // pass along z per column (ky, kx = lane), coefficients back in place
+            for (int ky = warp; ky < 32; ky += kFwdThreads / 32) {
+                int32_t v[32], o[32];
 #pragma unroll
-            for (int kz = 0; kz < 32; ++kz) quant_scatter(o[kz], kz, ky);
-        }
-        __syncthreads();
-        }
-        // compaction in scan order: thread owns positions [128 tid, 128 tid + 128)
-        const uint4 *Lv = reinterpret_cast<const uint4 *>(L + tid * 128);
-        uint32_t cnt = 0;
-#pragma unroll 4
-        for (int i = 0; i < 16; ++i) {
-            uint4 q = Lv[i];
-            uint32_t ws[4] = {q.x, q.y, q.z, q.w};
+                for (int z = 0; z < 32; ++z) v[z] = T[z * 1024 + swz(ky, lane)];
+                fdct32_line(v, o);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) cnt += ((ws[k] & 0xFFFFu) != 0) + ((ws[k] >> 16) != 0);
-        }
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) scanbuf[warp] = incl;
-        __syncthreads();
-        uint32_t base = 0, total = 0;
-#pragma unroll
-        for (int i = 0; i < kFwdThreads / 32; ++i) {
-            uint32_t v = scanbuf[i];
-            base += i < warp ? v : 0;
-            total += v;
-        }
-        base += incl - cnt;
-        uint32_t *dst = J.ent + t * (uint64_t)VCD_MAX_ENTRIES + base;
-        if (cnt) {
-#pragma unroll 4
-            for (int i = 0; i < 16; ++i) {
-                uint4 q = Lv[i];
-                uint32_t ws[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    uint32_t p = (uint32_t)(tid * 128 + i * 8 + k * 2);
-                    if (ws[k] & 0xFFFFu) *dst++ = p | (ws[k] << 16);
-                    if (ws[k] >> 16) *dst++ = (p + 1) | (ws[k] & 0xFFFF0000u);
-                }
+                for (int kz = 0; kz < 32; ++kz) T[kz * 1024 + swz(ky, lane)] = o[kz];
             }
+            __syncthreads();
+            auto tile = [&](uint32_t p, uint32_t r) {
+                const int32_t cf = T[((r >> 10) << 10) | swz((int)((r >> 5) & 31u), (int)(r & 31u))];
+                if (cached) cptr[p] = cf;   // kept in scan order
+                return cf;
+            };
+            total = quant_compact<kFwdThreads>(tile, J.scan, qdz, qrr, alt, L, wcnt, dst);
         }
         if (tid == 0) J.meta[t] = total | ((uint32_t)dc << 16);
-        __syncthreads();
+    }
+}
+
+// LOD0 atoms whose transform was kept: quantise in scan order and compact, with
+// a quarter of the shared memory of k_fwd (three CTAs per SM).
+constexpr size_t kQuantSmem = 32768 * sizeof(int16_t);
+
+__global__ void __launch_bounds__(kFwdThreads) k_quant_cached(FwdJob J) {
+    extern __shared__ int16_t lv[];
+    __shared__ float qdz[VCD_NCLASS], qrr[VCD_NCLASS];
+    __shared__ uint32_t alt[1024];
+    __shared__ uint32_t wcnt[kFwdThreads / 32];
+    const int tid = threadIdx.x;
+    for (int i = tid; i < 1024; i += kFwdThreads) alt[i] = J.alt_mask[i];
+    for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q[0].dz[i]; qrr[i] = J.q[0].rr[i]; }
+    __syncthreads();
+    for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
+        const uint64_t ca = J.first + t;
+        const uint32_t dcz = J.coef_dc[ca];
+        if (dcz & kMetaZero) {
+            if (tid == 0) J.meta[t] = kMetaZero;
+            continue;
+        }
+        const int32_t *cptr = J.coef + ca * 32768ull;
+        const uint32_t total = quant_compact<kFwdThreads>([&](uint32_t p, uint32_t) { return __ldcs(cptr + p); },
+                                                          J.scan, qdz, qrr, alt, lv, wcnt,
+                                                          J.ent + t * (uint64_t)VCD_MAX_ENTRIES);
+        if (tid == 0) J.meta[t] = total | ((dcz & 0xFFu) << 16);
     }
 }
 
@@ -311,6 +332,7 @@ void enc_set_smem() {
     static bool done = false;
     if (!done) {
         cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+        cudaFuncSetAttribute(k_quant_cached, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQuantSmem);
         done = true;
     }
 }
@@ -318,6 +340,13 @@ void enc_set_smem() {
 void launch_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, int num_sms,
                        cudaStream_t s) {
     k_downsample<<<num_sms * 8, 256, 0, s>>>(in, nx, ny, nz, out);
+}
+
+void launch_quant_cached(const FwdJob &J, int num_sms, cudaStream_t s) {
+    enc_set_smem();
+    if (!J.n_atoms) return;
+    const uint64_t cap = (uint64_t)num_sms * 3;
+    k_quant_cached<<<(unsigned)(J.n_atoms < cap ? J.n_atoms : cap), kFwdThreads, kQuantSmem, s>>>(J);
 }
 
 void launch_fwd(const FwdJob &J, int num_sms, cudaStream_t s) {

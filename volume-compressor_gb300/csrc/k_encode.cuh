@@ -45,13 +45,13 @@ struct FwdJob {
     uint64_t first;              // canonical index of this launch's first atom
     uint64_t n_atoms;
     const vcd_quant *q;          // per-LOD quantiser constants (device, [lod])
-    const uint16_t *rank_base;
+    const uint16_t *scan;        // scan position -> raster index
     const uint32_t *alt_mask;
     uint32_t *ent;               // per atom VCD_MAX_ENTRIES slots: scan position | level << 16
     uint32_t *meta;              // per atom
     // coefficient cache of canonical atoms [0, coef_n): 32768 i32 per atom in
-    // (kz, ky, kx) raster order, and dc | kMetaZero per atom; coef_store != 0
-    // fills it, else atoms below coef_n are quantised from it
+    // scan order, and dc | kMetaZero per atom; coef_store != 0 fills it, else
+    // atoms below coef_n are quantised from it
     int32_t *coef;
     uint32_t *coef_dc;
     uint64_t coef_n;
@@ -86,6 +86,8 @@ struct PlaceJob {
 void launch_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, int num_sms,
                        cudaStream_t s);
 void launch_fwd(const FwdJob &J, int num_sms, cudaStream_t s);
+// atoms that are all LOD0 with kept coefficients: quantise and compact only
+void launch_quant_cached(const FwdJob &J, int num_sms, cudaStream_t s);
 void launch_rc_encode(const RcJob &J, bool write, cudaStream_t s);
 void launch_consume(const PlaceJob &J, cudaStream_t s);
 void launch_slots(const PlaceJob &J, cudaStream_t s);

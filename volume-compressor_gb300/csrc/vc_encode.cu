@@ -66,7 +66,7 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
         F.first = c0;
         F.n_atoms = n;
         F.q = S.qtab;
-        F.rank_base = g_dev.tables->rank_base;
+        F.scan = g_dev.tables->scan;
         F.alt_mask = g_dev.tables->alt_mask;
         F.ent = S.ent;
         F.meta = S.meta;
@@ -77,7 +77,8 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
         const bool from_cache = S.coef && S.coef_valid && c0 + n <= S.coef_n;
         const bool prof = vcd_prof_on();
         if (prof) cudaEventRecord(S.c->ev[4], S.c->stream);
-        launch_fwd(F, g_dev.num_sms, S.c->stream);
+        if (from_cache) launch_quant_cached(F, g_dev.num_sms, S.c->stream);
+        else launch_fwd(F, g_dev.num_sms, S.c->stream);
         RcJob R;
         memset(&R, 0, sizeof R);
         R.n_atoms = n;
