@@ -67,7 +67,9 @@ typedef struct vcg_server vcg_server;
 vcg_server *vcg_server_create(vc_archive *a, uint64_t device_budget, uint32_t max_batch, int workers);
 // out: host memory of the box's size, valid until the ticket completes; returns a ticket >= 0, or -1
 int64_t vcg_server_submit(vcg_server *s, int lod, vc_box box, uint8_t *out);
-// blocks until the ticket is done; latency_us (optional) = submit-to-completion time
+// blocks until the ticket is done; latency_us (optional) = submit-to-completion
+// time. Each ticket is waited for once (its slot is then recycled; a second wait
+// is VC_ERR_RANGE); tickets that are never waited for keep their slots.
 vc_status vcg_server_wait(vcg_server *s, int64_t ticket, double *latency_us);
 void vcg_server_stats(vcg_server *s, uint64_t *batches, uint64_t *requests);
 // finishes all queued requests, then stops the workers

@@ -97,3 +97,16 @@ def test_server_host_logic_without_device(vc, golden):
         a.server(device_budget=0)
     with a.server() as srv:
         assert srv.wait(5)[0] == vc.VC_ERR_RANGE   # ticket never issued
+    # slots of waited tickets are recycled: thousands of tickets, a second wait is refused
+    out = np.zeros(32768, np.uint8)
+    with a.server(device_budget=1 << 20, max_batch=16, workers=2) as srv:
+        first = srv.submit(0, (0, 0, 0, 32, 32, 32), out)
+        assert srv.wait(first)[0] in (vc.VC_OK, vc.VC_ERR_IO)
+        assert srv.wait(first)[0] == vc.VC_ERR_RANGE
+        for _ in range(30):
+            tix = [srv.submit(0, (0, 0, 0, 32, 32, 32), out) for _ in range(100)]
+            assert all(t >= 0 for t in tix)
+            assert {srv.wait(t)[0] for t in tix} <= {vc.VC_OK, vc.VC_ERR_IO}
+        assert srv.wait(first)[0] == vc.VC_ERR_RANGE
+        batches, done = srv.stats()
+        assert done == 3001

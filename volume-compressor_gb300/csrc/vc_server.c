@@ -25,7 +25,7 @@ typedef struct {
     uint64_t cost;          // device bytes the request holds while decoding
     double t_submit, t_done;
     vc_status status;
-    int state;              // 0 queued, 1 running, 2 done
+    int state;              // 0 queued, 1 running, 2 done, 3 done and waited for
 } srv_req;
 
 typedef struct vcg_server {
@@ -36,11 +36,14 @@ typedef struct vcg_server {
     pthread_t th[8];
     pthread_mutex_t mu;
     pthread_cond_t work_cv, done_cv;
-    srv_req *reqs;          // ticket -> request (grows)
-    uint64_t cap, n;        // tickets issued
+    srv_req *reqs;          // ticket t is reqs[t - base]
+    uint64_t cap, base, n;  // slots, ticket of reqs[0], tickets issued
     uint64_t head;          // first ticket not yet taken by a worker
+    uint64_t lo;            // every ticket below lo has been waited for
     uint64_t batches, batched_reqs;
 } vcg_server;
+
+static srv_req *slot(vcg_server *s, uint64_t ticket) { return &s->reqs[ticket - s->base]; }
 
 static double now_us(void) {
     struct timespec ts;
@@ -71,7 +74,7 @@ static void *worker(void *arg) {
         uint32_t k = 0;
         uint64_t take = 0;
         while (s->head < s->n && k < s->max_batch) {
-            srv_req *r = &s->reqs[s->head];
+            srv_req *r = slot(s, s->head);
             if (s->in_use + take + r->cost > s->budget && (k > 0 || s->in_use > 0)) break;
             r->state = 1;
             batch[k] = r->req;
@@ -90,7 +93,7 @@ static void *worker(void *arg) {
         double t = now_us();
         pthread_mutex_lock(&s->mu);
         for (uint32_t i = 0; i < k; ++i) {
-            srv_req *r = &s->reqs[tix[i]];
+            srv_req *r = slot(s, tix[i]);
             r->status = rc != VC_OK ? rc : st[i];
             r->t_done = t;
             r->state = 2;
@@ -136,13 +139,19 @@ VC_API vcg_server *vcg_server_create(vc_archive *a, uint64_t device_budget, uint
 VC_API int64_t vcg_server_submit(vcg_server *s, int lod, vc_box box, uint8_t *out) {
     if (!s) return -1;
     pthread_mutex_lock(&s->mu);
-    if (s->n == s->cap) {
-        srv_req *t = (srv_req *)realloc(s->reqs, 2 * s->cap * sizeof(srv_req));
-        if (!t) { pthread_mutex_unlock(&s->mu); return -1; }
-        s->reqs = t;
-        s->cap *= 2;
+    if (s->n - s->base == s->cap) {
+        if (s->lo - s->base >= s->cap / 2) {   // recycle the slots of waited tickets
+            const uint64_t drop = s->lo - s->base;
+            memmove(s->reqs, s->reqs + drop, (size_t)(s->cap - drop) * sizeof(srv_req));
+            s->base = s->lo;
+        } else {
+            srv_req *t = (srv_req *)realloc(s->reqs, 2 * s->cap * sizeof(srv_req));
+            if (!t) { pthread_mutex_unlock(&s->mu); return -1; }
+            s->reqs = t;
+            s->cap *= 2;
+        }
     }
-    srv_req *r = &s->reqs[s->n];
+    srv_req *r = slot(s, s->n);
     memset(r, 0, sizeof *r);
     r->req.lod = lod;
     r->req.box = box;
@@ -156,14 +165,21 @@ VC_API int64_t vcg_server_submit(vcg_server *s, int lod, vc_box box, uint8_t *ou
 }
 
 // Block until the ticket is decoded; returns its status (vc_decode_region's),
-// and the submit-to-completion latency in microseconds.
+// and the submit-to-completion latency in microseconds. A ticket can be waited
+// for once: its slot is recycled afterwards (VC_ERR_RANGE on a second wait).
 VC_API vc_status vcg_server_wait(vcg_server *s, int64_t ticket, double *latency_us) {
     if (!s || ticket < 0) return VC_ERR_RANGE;
     pthread_mutex_lock(&s->mu);
-    if ((uint64_t)ticket >= s->n) { pthread_mutex_unlock(&s->mu); return VC_ERR_RANGE; }
-    while (s->reqs[ticket].state != 2) pthread_cond_wait(&s->done_cv, &s->mu);
-    vc_status st = s->reqs[ticket].status;
-    if (latency_us) *latency_us = s->reqs[ticket].t_done - s->reqs[ticket].t_submit;
+    if ((uint64_t)ticket >= s->n || (uint64_t)ticket < s->base || slot(s, (uint64_t)ticket)->state == 3) {
+        pthread_mutex_unlock(&s->mu);
+        return VC_ERR_RANGE;
+    }
+    while (slot(s, (uint64_t)ticket)->state != 2) pthread_cond_wait(&s->done_cv, &s->mu);
+    srv_req *r = slot(s, (uint64_t)ticket);
+    vc_status st = r->status;
+    if (latency_us) *latency_us = r->t_done - r->t_submit;
+    r->state = 3;
+    while (s->lo < s->n && slot(s, s->lo)->state == 3) ++s->lo;
     pthread_mutex_unlock(&s->mu);
     return st;
 }
