@@ -71,7 +71,7 @@ static void ctx_free(void *p) {
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     if (c->copy_stream) {
-        for (int i = 0; i < 8; ++i) cudaEventDestroy(c->chunk_ev[i]);
+        for (int i = 0; i < 16; ++i) cudaEventDestroy(c->chunk_ev[i]);
         cudaStreamDestroy(c->copy_stream);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -270,8 +270,8 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
     StageEvents ev;
     memcpy(ev.ev, c->ev, sizeof ev.ev);
     uint64_t ctl_h[2] = {0xFFFFFFFFull, 0};
-    // Large outputs to pinned host memory: the inverse transform runs in slabs of
-    // atom layers and each finished slab is copied out on a second stream while
+    // Large outputs to pinned host memory: the inverse transform runs in up to 16
+    // slabs of atom layers and each finished slab is copied out on a second stream while
     // the next one is transformed. The range decode finishes first, so a stream
     // with a malformed atom is known before any byte reaches the caller.
     // (only when every atom of the box is decoded: a box cut short by a bad
@@ -287,7 +287,7 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
                 c->copy_stream = NULL;
                 piped = false;
             } else {
-                for (int i = 0; i < 8; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
+                for (int i = 0; i < 16; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
             }
         }
     }
@@ -304,7 +304,7 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
             piped = false;
         } else {
             const uint64_t plane = (uint64_t)J.ox * J.oy;
-            const uint64_t per = (layers + 7) / 8;
+            const uint64_t per = (layers + 15) / 16;
             int k = 0;
             for (uint64_t l0 = 0; l0 < layers; l0 += per, ++k) {
                 const uint64_t l1 = l0 + per < layers ? l0 + per : layers;

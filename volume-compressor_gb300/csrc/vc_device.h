@@ -29,7 +29,7 @@ struct vcd_ctx {
     unsigned char batch_key[512];   // kernel parameters + shape + grid capacity the graph was captured with
     // copy-out overlapped with the inverse transform (created on first use)
     cudaStream_t copy_stream;
-    cudaEvent_t chunk_ev[8];
+    cudaEvent_t chunk_ev[16];
 };
 
 // Kernel statistics, accumulated while profiling is enabled (vcg_profile_enable).
