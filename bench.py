@@ -403,7 +403,26 @@ def config2_sweep(dvol, dims, peak, targets=(10.0, 50.0, 100.0)):
             if g:
                 lod_ok.append(hashlib.sha256(buf.download(lx * ly * lz).tobytes()).hexdigest() == g["lod_sha256"][lod])
             buf.free()
+        # the v2 container: repacked on the device, then decoded through its directory
+        s, v2 = a.repack_v2()
+        assert s == 0, vc.last_error()
+        s, _ = a.repack_v2()
+        rp_ms = vc.last_call_ms()
         a.close()
+        b = vc.Archive(v2)
+        assert b.make_resident() == 0
+        buf = vc.DeviceBuffer(nx * ny * nz)
+        assert b.decode_lod_device(0, buf) == 0
+        ms = []
+        for _ in range(3):
+            assert b.decode_lod_device(0, buf) == 0
+            ms.append(vc.last_call_ms())
+        v2_ok = (hashlib.sha256(buf.download(nx * ny * nz).tobytes()).hexdigest() == g["lod_sha256"][0]) if g else None
+        buf.free()
+        b.close()
+        row["v2"] = {"bytes": len(v2), "repack_ms": rp_ms, "repack_GBps": len(data) / (rp_ms / 1e3) / 1e9,
+                     "lod0_decode_GBps": nx * ny * nz / (statistics.median(ms) / 1e3) / 1e9,
+                     "lod0_matches_reference": v2_ok}
         row["decode_lods"] = lods
         row["lods_match_reference"] = all(lod_ok) if g else None
         res[f"t{int(t)}"] = row

@@ -75,6 +75,14 @@ void vcg_server_stats(vcg_server *s, uint64_t *batches, uint64_t *requests);
 // finishes all queued requests, then stops the workers
 void vcg_server_destroy(vcg_server *s);
 
+// Rewrite an archive (v1 or v2) into the v2 container, byte-identical to the
+// reference's repack tool (tools/vc_repack.c): region directory + one
+// contiguous blob per region with a present atom, coarse LOD first, payloads
+// copied verbatim. The image is assembled on the device from the resident
+// archive; *out_archive is malloc'd. VC_ERR_FORMAT for an archive with a payload
+// range outside the file.
+vc_status vcg_repack_v2(vc_archive *a, uint8_t **out_archive, size_t *out_len);
+
 // Resolve the archive's atom table and copy archive + table into device
 // memory now (otherwise done on the first decode).
 vc_status vcg_make_resident(vc_archive *a);

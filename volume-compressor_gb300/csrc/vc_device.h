@@ -11,7 +11,7 @@ enum {
     VCD_BUF_VOL, VCD_BUF_PYR, VCD_BUF_EENT, VCD_BUF_EMETA, VCD_BUF_LEN, VCD_BUF_POS, VCD_BUF_ARC,
     VCD_BUF_BEST, VCD_BUF_RED,
     VCD_BUF_BUA, VCD_BUF_BDST, VCD_BUF_BREQ, VCD_BUF_BOFF, VCD_BUF_BCNT, VCD_BUF_BENT, VCD_BUF_BCTL, VCD_BUF_BOUT,
-    VCD_BUF_BPIN, VCD_BUF_COEF,
+    VCD_BUF_BPIN, VCD_BUF_COEF, VCD_BUF_RPK, VCD_BUF_RPKREC,
     VCD_NBUF
 };
 

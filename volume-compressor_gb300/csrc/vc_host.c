@@ -638,3 +638,115 @@ VC_API vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dim
     if (!base_q) return VC_ERR_RANGE;
     return encode_common(vol, vol_on_device, dims, target_ratio, base_q, out_archive, out_len, NULL);
 }
+
+// ---------------------------------------------------------------------------
+// Repack into the v2 container (tools/vc_repack.c:96-177, layout
+// src/vc/vc.c:706-718): [128-byte header][region directory, 16 B per region in
+// canonical order][4 KiB-aligned blobs]. Regions are laid out coarse LOD first,
+// raster order within a LOD; a region with a present atom gets a blob of its
+// 512 KiB slot array followed by its payloads in slot order, copied verbatim.
+// The image is assembled on the device from the resident archive.
+// ---------------------------------------------------------------------------
+VC_API vc_status vcg_repack_v2(vc_archive *a, uint8_t **out_archive, size_t *out_len) {
+    if (!a || !out_archive || !out_len) return VC_ERR_RANGE;
+    *out_archive = NULL;
+    *out_len = 0;
+    if (make_resident(a) != 0) return VC_ERR_IO;
+    uint64_t prefix[VC_NLOD + 1], total_regions = 0;
+    for (int l = 0; l < a->nlod; ++l) {
+        uint32_t z, y, x;
+        region_grid(a->d0, l, &z, &y, &x);
+        prefix[l] = total_regions;
+        total_regions += (uint64_t)z * y * x;
+    }
+    const uint64_t dir_off = FILE_HDR, head_len = dir_off + total_regions * 16;
+    const uint64_t blobs_off = (head_len + 4095) & ~4095ull;
+    uint8_t *head = (uint8_t *)calloc(head_len, 1);
+    uint64_t cap = 1024, n = 0;
+    vcd_repack_rec *recs = (vcd_repack_rec *)malloc(cap * sizeof(vcd_repack_rec));
+    if (!head || !recs) { free(head); free(recs); return VC_ERR_OOM; }
+    vc_status rc = VC_OK;
+    uint64_t cursor = blobs_off;
+    for (int l = a->nlod - 1; l >= 0 && rc == VC_OK; --l) {
+        uint32_t nrz, nry, nrx;
+        region_grid(a->d0, l, &nrz, &nry, &nrx);
+        for (uint32_t rz = 0; rz < nrz && rc == VC_OK; ++rz)
+            for (uint32_t ry = 0; ry < nry && rc == VC_OK; ++ry)
+                for (uint32_t rx = 0; rx < nrx && rc == VC_OK; ++rx) {
+                    const uint64_t ri = prefix[l] + ((uint64_t)rz * nry + ry) * nrx + rx;
+                    uint8_t *e = head + dir_off + ri * 16;
+                    uint64_t pay = 0;
+                    int any_present = 0, any_zero = 0;
+                    for (uint32_t s = 0; s < R_ATOMS * R_ATOMS * R_ATOMS; ++s) {
+                        const uint32_t az = rz * R_ATOMS + s / (R_ATOMS * R_ATOMS),
+                                       ay = ry * R_ATOMS + (s / R_ATOMS) % R_ATOMS, ax = rx * R_ATOMS + s % R_ATOMS;
+                        uint64_t off;
+                        uint32_t len;
+                        const vc_cover cov = vc_atom_payload_range(a, l, az, ay, ax, &off, &len);
+                        if (cov == VC_PRESENT) {
+                            if (len < 1 || off > a->len || len > a->len - off) { rc = VC_ERR_FORMAT; break; }
+                            any_present = 1;
+                            pay += len;
+                        } else if (cov == VC_KNOWN_ZERO) {
+                            any_zero = 1;
+                        }
+                    }
+                    if (rc != VC_OK) break;
+                    if (!any_present) {
+                        const uint32_t fl = any_zero ? 1u : 0u;   // ZERO / ABSENT
+                        memcpy(e + 12, &fl, 4);
+                        continue;
+                    }
+                    const uint64_t blob = cursor, blen = L2_BYTES + pay;
+                    const uint32_t blen32 = (uint32_t)blen, fl = 2u;   // DATA
+                    memcpy(e, &blob, 8);
+                    memcpy(e + 8, &blen32, 4);
+                    memcpy(e + 12, &fl, 4);
+                    uint64_t paycur = blob + L2_BYTES;
+                    for (uint32_t s = 0; s < R_ATOMS * R_ATOMS * R_ATOMS; ++s) {
+                        const uint32_t az = rz * R_ATOMS + s / (R_ATOMS * R_ATOMS),
+                                       ay = ry * R_ATOMS + (s / R_ATOMS) % R_ATOMS, ax = rx * R_ATOMS + s % R_ATOMS;
+                        uint64_t off;
+                        uint32_t len;
+                        const vc_cover cov = vc_atom_payload_range(a, l, az, ay, ax, &off, &len);
+                        if (cov == VC_ABSENT) continue;
+                        if (n == cap) {
+                            vcd_repack_rec *t = (vcd_repack_rec *)realloc(recs, 2 * cap * sizeof(vcd_repack_rec));
+                            if (!t) { rc = VC_ERR_OOM; break; }
+                            recs = t;
+                            cap *= 2;
+                        }
+                        vcd_repack_rec *r = &recs[n++];
+                        r->slot_dst = blob + (uint64_t)s * 16;
+                        if (cov == VC_PRESENT) {
+                            r->src = off; r->pay_dst = paycur; r->len = len; r->flags = 1;
+                            paycur += len;
+                        } else {
+                            r->src = 0; r->pay_dst = 0; r->len = 0; r->flags = 2;
+                        }
+                    }
+                    cursor += blen;
+                }
+    }
+    if (rc == VC_OK) {
+        const uint32_t w[6] = {MAGIC, 2u, 32u, 0u, R_ATOMS, (uint32_t)a->nlod};
+        memcpy(head, w, sizeof w);
+        const uint32_t dims[3] = {a->d0.nx, a->d0.ny, a->d0.nz};
+        memcpy(head + 24, dims, sizeof dims);
+        memcpy(head + 36, a->buf + 36, 4);   // target ratio
+        const uint64_t h64[3] = {dir_off, total_regions, cursor};
+        memcpy(head + 40, h64, sizeof h64);
+        memcpy(head + 72, a->buf + 72, 4 * VC_NLOD);   // base_q per LOD
+        uint8_t *res = (uint8_t *)malloc(cursor);
+        if (!res) {
+            rc = VC_ERR_OOM;
+        } else {
+            const int e = vcd_repack(a->dev, head, head_len, cursor, recs, n, res);
+            if (e) { free(res); rc = (vc_status)e; report("repack: %s", vcd_last_error()); }
+            else { *out_archive = res; *out_len = cursor; }
+        }
+    }
+    free(head);
+    free(recs);
+    return rc;
+}

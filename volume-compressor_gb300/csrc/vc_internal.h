@@ -118,6 +118,19 @@ typedef struct {
 int  vcd_encode(const uint8_t *vol, int vol_on_device, vcd_encode_info *info, uint8_t **out,
                 size_t *out_len);
 
+// Repack into the v2 container (device): one record per non-absent atom slot of
+// the output. flags 1 = present (slot [pay_dst][len][1][dc = first payload
+// byte], payload src..src+len of the resident archive copied to pay_dst),
+// flags 2 = known zero (slot byte 12 = 2). head (header + region directory,
+// head_len bytes) goes to offset 0; everything else of the total_len-byte image
+// is zero. The image is copied into host_out.
+typedef struct {
+    uint64_t slot_dst, src, pay_dst;
+    uint32_t len, flags;
+} vcd_repack_rec;
+int  vcd_repack(vcd_archive *d, const uint8_t *head, uint64_t head_len, uint64_t total_len,
+                const vcd_repack_rec *recs, uint64_t n_recs, uint8_t *host_out);
+
 // ---- host helpers shared with the device layer (vc_host.c) ----------------
 void vch_tables(vcd_tables *t);
 void vch_quant_consts(float base_q, vcd_quant *q);

@@ -22,7 +22,7 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
               "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_set_rc_scalar_warps", "vcg_dct_forward", "vcg_dct_inverse",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps", "vcg_dct_forward", "vcg_dct_inverse",
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
@@ -168,6 +168,7 @@ def lib():
         L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
         L.vcg_batch_shape.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
         L.vcg_set_batch_shape.argtypes = [ctypes.c_int] * 3
+        L.vcg_repack_v2.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_size_t)]
         L.vcg_set_rc_scalar_warps.argtypes = [ctypes.c_int]
         L.vcg_dct_forward.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, P, ctypes.POINTER(ctypes.c_uint32)]
         L.vcg_dct_inverse.argtypes = [P, P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
@@ -386,6 +387,16 @@ class Archive:
         st = np.zeros(len(reqs), np.int32)
         s = lib().vcg_decode_regions(self.h, len(reqs), arr, 1 if on_device else 0, ptr(st))
         return s, st
+
+    def repack_v2(self):
+        """vcg_repack_v2: (status, v2 archive bytes)."""
+        out, n = P(), ctypes.c_size_t()
+        s = lib().vcg_repack_v2(self.h, ctypes.byref(out), ctypes.byref(n))
+        if s:
+            return s, None
+        data = ctypes.string_at(out, n.value)
+        _libc.free(out)
+        return s, data
 
     def server(self, device_budget=1 << 30, max_batch=4096, workers=2):
         return Server(self, device_budget, max_batch, workers)
