@@ -423,9 +423,51 @@ def config2_sweep(dvol, dims, peak, targets=(10.0, 50.0, 100.0)):
         row["v2"] = {"bytes": len(v2), "repack_ms": rp_ms, "repack_GBps": len(data) / (rp_ms / 1e3) / 1e9,
                      "lod0_decode_GBps": nx * ny * nz / (statistics.median(ms) / 1e3) / 1e9,
                      "lod0_matches_reference": v2_ok}
+        want0 = g["lod_sha256"][0] if g else None
+        row["streamed_lod0"] = {"v1": streamed_lod0(vc, data, dims, want0), "v2": streamed_lod0(vc, v2, dims, want0)}
         row["decode_lods"] = lods
         row["lods_match_reference"] = all(lod_ok) if g else None
         res[f"t{int(t)}"] = row
+    return res
+
+
+def streamed_lod0(vc, data, dims, want, threads=(1, 8), reps=3):
+    """LOD0 of `data` through vc_open_streaming: the library's memory byte
+    source over the archive in pageable host memory (the stand-in for a cache of
+    a remote object), payloads pulled through the callback into pinned staging
+    and uploaded while the next ones are read, output to pinned host memory.
+    Wall clock of vc_open_streaming + vc_decode_lod + vc_close, median of reps
+    after one warm-up, per number of fetch threads."""
+    import ctypes
+    import hashlib
+    import numpy as np
+    L = vc.lib()
+    nx, ny, nz = dims
+    nbytes = nx * ny * nz
+    src_buf = ctypes.create_string_buffer(bytes(data), len(data))
+    ho = L.vcg_alloc_host(nbytes)
+    out = np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(ho))
+    d = vc.Dims()
+    res = {}
+    for th in threads:
+        prev = vc.set_stream_threads(th)
+        ts = []
+        for k in range(reps + 1):
+            src = vc.MemorySource(ctypes.addressof(src_buf), len(data), 0, 0)
+            t0 = time.perf_counter()
+            h = L.vc_open_streaming(ctypes.cast(L.vcg_memory_read, ctypes.c_void_p), ctypes.addressof(src), len(data))
+            st = L.vc_decode_lod(h, 0, ho, ctypes.byref(d))
+            L.vc_close(h)
+            t1 = time.perf_counter()
+            assert st == 0, vc.last_error()
+            if k:
+                ts.append(t1 - t0)
+        vc.set_stream_threads(prev)
+        m = statistics.median(ts)
+        res[f"threads{th}"] = {"ms": m * 1e3, "GBps": nbytes / m / 1e9, "reads": src.reads, "bytes_read": src.bytes,
+                               "matches_reference": (hashlib.sha256(out).hexdigest() == want) if want else None}
+    del out
+    L.vcg_free_host(ho)
     return res
 
 

@@ -67,6 +67,19 @@ vc_status vc_encode(const uint8_t *vol, vc_dims dims, float target_ratio,
 // The archive bytes are copied into device memory on first decode.
 vc_archive *vc_open(const uint8_t *archive, size_t len);
 
+// src/vc/vc.h:108-112 — byte source of a streaming archive: fill dst with
+// exactly len bytes from archive offset off; return VC_OK on success.
+typedef vc_status (*vc_read_fn)(void *ud, uint64_t off, uint32_t len, uint8_t *dst);
+
+// src/vc/vc.h:118 — open an archive without holding it: the header here, and
+// the index entries, slots and payloads each decode needs, are pulled through
+// read on demand. total_len is the archive's size. Results equal vc_open's on
+// the same bytes. As in the reference, an index entry or slot whose read fails
+// is absent, and a payload whose read fails, or that is longer than 131136
+// bytes, makes its atom VC_ERR_FORMAT. read is called only from the decoding
+// thread unless vcg_set_stream_threads allows more; it must outlive the handle.
+vc_archive *vc_open_streaming(vc_read_fn read, void *ud, uint64_t total_len);
+
 // src/vc/vc.h:120 — NULL is allowed.
 void vc_close(vc_archive *a);
 

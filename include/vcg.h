@@ -84,8 +84,27 @@ void vcg_server_destroy(vcg_server *s);
 vc_status vcg_repack_v2(vc_archive *a, uint8_t **out_archive, size_t *out_len);
 
 // Resolve the archive's atom table and copy archive + table into device
-// memory now (otherwise done on the first decode).
+// memory now (otherwise done on the first decode). A streaming archive is
+// first pulled whole through its read callback (VC_ERR_IO if a read fails; it
+// then stays streaming); batched decode, the server and repack make it
+// resident this way on their first call, while vc_decode_* of a streaming
+// archive that is not resident pull only what the box needs.
 vc_status vcg_make_resident(vc_archive *a);
+
+// Host threads that call a streaming archive's read callback during one
+// decode: 1 (the default) keeps every call on the decoding thread; up to 64
+// for callbacks that are safe to call concurrently. Returns the previous value.
+int vcg_set_stream_threads(int n);
+
+// A vc_read_fn byte source over a host buffer (tests, benchmarks): ud points
+// to a vcg_memory_source; reads and bytes count the calls and bytes served.
+// A range outside [0, len) returns VC_ERR_FORMAT.
+typedef struct {
+    const uint8_t *buf;
+    uint64_t len;
+    uint64_t reads, bytes;
+} vcg_memory_source;
+vc_status vcg_memory_read(void *ud, uint64_t off, uint32_t len, uint8_t *dst);
 
 // vc_encode with the volume already in device memory; *q0 (optional)
 // receives the LOD0 base_q chosen by rate control.

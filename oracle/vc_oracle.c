@@ -661,7 +661,8 @@ void orc_free(void *p) { free(p); }
 // Reader (:1247-1555)
 // ---------------------------------------------------------------------------
 struct orc_archive {
-    const uint8_t *buf; size_t len;
+    const uint8_t *buf; size_t len;     // buf == NULL: streaming (read / ud)
+    orc_read_fn read; void *ud;
     orc_dims d0; int nlod, version;
     uint64_t l1_off, l1_cap, dir_off, region_prefix[9];
     float base_q[8];
@@ -670,6 +671,20 @@ struct orc_archive {
 static void region_grid(orc_dims d0, int lod, uint32_t *nrz, uint32_t *nry, uint32_t *nrx) {
     orc_dims d = orc_lod_dims_of(d0, lod);
     *nrx = ((d.nx + 31) / 32 + 31) / 32; *nry = ((d.ny + 31) / 32 + 31) / 32; *nrz = ((d.nz + 31) / 32 + 31) / 32;
+}
+
+// Streaming open (:1329-1338): the header through the callback, then the same
+// validation as orc_open; every later read goes through rd().
+orc_archive *orc_open_streaming(orc_read_fn read, void *ud, uint64_t total_len) {
+    if (!read || total_len < FILE_HDR) return NULL;
+    uint8_t hdr[FILE_HDR];
+    if (read(ud, 0, FILE_HDR, hdr) != ORC_OK) return NULL;
+    orc_archive *a = orc_open(hdr, total_len);
+    if (!a) return NULL;
+    a->buf = NULL;
+    a->read = read;
+    a->ud = ud;
+    return a;
 }
 
 orc_archive *orc_open(const uint8_t *buf, size_t len) {   // :1285-1323
@@ -717,6 +732,15 @@ int orc_lod_dims(const orc_archive *a, int lod, orc_dims *out) {
 // bytes [off, off+n) inside the archive (the reference's test at :1266)
 static int in_file(const orc_archive *a, uint64_t off, uint64_t n) { return off + n <= a->len; }
 
+// Fetch [off, off + n) (:1262-1267): a flat archive copies from its buffer, a
+// streaming one asks the callback. 0 on success.
+static int rd(const orc_archive *a, uint64_t off, uint32_t n, uint8_t *dst) {
+    if (a->read) return a->read(a->ud, off, n, dst) == ORC_OK ? 0 : -1;
+    if (!in_file(a, off, n)) return -1;
+    memcpy(dst, a->buf + off, n);
+    return 0;
+}
+
 static int resolve(const orc_archive *a, int lod, uint32_t az, uint32_t ay, uint32_t ax,
                    uint64_t *off, uint32_t *len, uint8_t *dc) {   // :1349-1402
     uint64_t slot_idx = (((uint64_t)(az & 31) * 32 + (ay & 31)) * 32 + (ax & 31));
@@ -727,31 +751,32 @@ static int resolve(const orc_archive *a, int lod, uint32_t az, uint32_t ay, uint
         if (rz >= nrz || ry >= nry || rx >= nrx) return 0;
         uint64_t ri = a->region_prefix[lod] + ((uint64_t)rz * nry + ry) * nrx + rx;
         if (ri >= a->region_prefix[a->nlod]) return 0;
-        uint64_t eo = a->dir_off + ri * 16;
-        if (!in_file(a, eo, 16)) return 0;
-        uint32_t fl = rd32(a->buf + eo + 12);
+        uint8_t e[16];
+        if (rd(a, a->dir_off + ri * 16, 16, e)) return 0;
+        uint32_t fl = rd32(e + 12);
         if (fl == 0) return 0;
         if (fl == 1) return 2;
-        blk = rd64(a->buf + eo);
+        blk = rd64(e);
     } else {
         uint64_t key = region_key(lod, az / 32, ay / 32, ax / 32);
         uint64_t mask = a->l1_cap - 1, i = mix64(key) & mask;
         // bounded probe: a table with no empty bucket and no match is treated as absent
         for (uint64_t step = 0;; ++step) {
             if (step >= a->l1_cap) return 0;
-            uint64_t eo = a->l1_off + i * 16;
-            if (!in_file(a, eo, 16)) return 0;
-            uint64_t bref = rd64(a->buf + eo + 8);
+            uint8_t e[16];
+            if (rd(a, a->l1_off + i * 16, 16, e)) return 0;
+            uint64_t bref = rd64(e + 8);
             if (!bref) return 0;
-            if (rd64(a->buf + eo) == key) { blk = bref; break; }
+            if (rd64(e) == key) { blk = bref; break; }
             i = (i + 1) & mask;
         }
         if (blk == 1) return 2;
     }
     if (blk + L2_BYTES > a->len || blk > a->len) return 0;
-    uint64_t so = blk + slot_idx * 16;
-    uint8_t fl = a->buf[so + 12];
-    if (fl == 1) { *off = rd64(a->buf + so); *len = rd32(a->buf + so + 8); *dc = a->buf[so + 13]; }
+    uint8_t sl[16];
+    if (rd(a, blk + slot_idx * 16, 16, sl)) return 0;   // :1367
+    uint8_t fl = sl[12];
+    if (fl == 1) { *off = rd64(sl); *len = rd32(sl + 8); *dc = sl[13]; }
     return fl;
 }
 
@@ -763,8 +788,20 @@ static int decode_atom_raw(orc_archive *a, int lod, uint32_t ax, uint32_t ay, ui
             memset(out, 0, N3);
             return ORC_ERR_FORMAT;
         }
-        if (orc_decode_atom_payload(a->buf + off, len, a->base_q[lod], out)) return ORC_ERR_FORMAT;
-        return ORC_OK;
+        if (!a->read) {
+            if (orc_decode_atom_payload(a->buf + off, len, a->base_q[lod], out)) return ORC_ERR_FORMAT;
+            return ORC_OK;
+        }
+        // streaming payload (:1274-1280): at most the reference's scratch of 4 * 32768 + 64 bytes
+        uint8_t *pay = len <= 4u * N3 + 64u ? (uint8_t *)malloc(len) : NULL;
+        if (!pay || rd(a, off, len, pay)) {
+            free(pay);
+            memset(out, 0, N3);
+            return ORC_ERR_FORMAT;
+        }
+        int bad = orc_decode_atom_payload(pay, len, a->base_q[lod], out);
+        free(pay);
+        return bad ? ORC_ERR_FORMAT : ORC_OK;
     }
     memset(out, 0, N3);
     return ORC_OK;

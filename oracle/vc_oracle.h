@@ -59,6 +59,8 @@ void     orc_free(void *p);
 // ---- reader (src/vc/vc.c:1285-1555)
 typedef struct orc_archive orc_archive;
 orc_archive *orc_open(const uint8_t *buf, size_t len);
+typedef int (*orc_read_fn)(void *ud, uint64_t off, uint32_t len, uint8_t *dst);   // 0 = ok
+orc_archive *orc_open_streaming(orc_read_fn read, void *ud, uint64_t total_len);
 void     orc_close(orc_archive *a);
 int      orc_lod_dims(const orc_archive *a, int lod, orc_dims *out);
 int      orc_nlod_of(const orc_archive *a);

@@ -53,6 +53,8 @@ def lib():
         L.vc_writer_close.argtypes = [ctypes.c_void_p]
         L.vc_open.restype = ctypes.c_void_p
         L.vc_open.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+        L.vc_open_streaming.restype = ctypes.c_void_p
+        L.vc_open_streaming.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
         L.vc_close.argtypes = [ctypes.c_void_p]
         L.vc_lod_dims.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Dims)]
         L.vc_decode_atom.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -246,3 +248,21 @@ class RefArchive:
 
     def coverage(self, lod, az, ay, ax):
         return lib().vc_atom_coverage(self.h, lod, az, ay, ax)
+
+
+READ_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p)
+
+
+class RefStreamingArchive(RefArchive):
+    """The reference's vc_open_streaming over read(off, n) -> n bytes, or None
+    for a failed read (returned to the reference as VC_ERR_FORMAT)."""
+
+    def __init__(self, read, total_len):
+        def cb(ud, off, n, dst):
+            b = read(off, n)
+            if b is None or len(b) != n:
+                return 1
+            ctypes.memmove(dst, bytes(b), n)
+            return 0
+        self._cb = READ_FN(cb)
+        self.h = lib().vc_open_streaming(ctypes.cast(self._cb, ctypes.c_void_p), None, total_len)

@@ -59,6 +59,8 @@ def lib():
         L.orc_free.argtypes = [P]
         L.orc_open.restype = P
         L.orc_open.argtypes = [P, ctypes.c_size_t]
+        L.orc_open_streaming.restype = P
+        L.orc_open_streaming.argtypes = [P, P, ctypes.c_uint64]
         L.orc_close.argtypes = [P]
         L.orc_lod_dims.argtypes = [P, ctypes.c_int, ctypes.POINTER(Dims)]
         L.orc_decode_atom.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
@@ -179,3 +181,20 @@ class Archive:
         o, l = ctypes.c_uint64(), ctypes.c_uint32()
         c = lib().orc_atom_payload_range(self.h, lod, az, ay, ax, ctypes.byref(o), ctypes.byref(l))
         return c, o.value, l.value
+READ_FN = ctypes.CFUNCTYPE(ctypes.c_int, P, ctypes.c_uint64, ctypes.c_uint32, P)
+
+
+class StreamingArchive(Archive):
+    """orc_open_streaming over read(off, n) -> n bytes, or None for a failed read."""
+
+    def __init__(self, read, total_len):
+        def cb(ud, off, n, dst):
+            b = read(off, n)
+            if b is None or len(b) != n:
+                return 1
+            ctypes.memmove(dst, bytes(b), n)
+            return 0
+        self._cb = READ_FN(cb)
+        self.h = lib().orc_open_streaming(ctypes.cast(self._cb, P), None, total_len)
+
+

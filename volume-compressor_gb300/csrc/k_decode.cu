@@ -31,7 +31,7 @@ __global__ void k_caps(DecodeJob J) {
     if (t >= J.n_atoms) return;
     uint32_t az, ay, ax;
     box_atom(J, t, az, ay, ax);
-    vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
+    vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
     uint64_t cap = 0;
     if (e.kind == VCD_PRESENT) {
         cap = 8ull * (e.len - 1) + 64ull;
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G) {
     if (lane < G && t < J.n_atoms) {
         uint32_t az, ay, ax;
         box_atom(J, t, az, ay, ax);
-        e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
+        e = J.atoms[job_atom(J, t, az, ay, ax)];
         active = e.kind == VCD_PRESENT;
         if (!active) J.cnt[t] = 0;
     }
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
     for (uint64_t t = J.t_lo + blockIdx.x; t < J.t_hi; t += gridDim.x) {
         uint32_t az, ay, ax;
         box_atom(J, t, az, ay, ax);
-        const vcd_atom e = J.atoms[((uint64_t)az * J.acy + ay) * J.acx + ax];
+        const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
         Crop k;
         const uint32_t gx = ax * 32, gy = ay * 32, gz = az * 32;
         k.set(gx, gy, gz, J.x0, J.y0, J.z0, J.x1, J.y1, J.z1);

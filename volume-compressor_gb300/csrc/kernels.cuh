@@ -31,7 +31,13 @@ struct DecodeJob {
     unsigned long long *nnz_total;   // coefficient-list entries written (sum over atoms)
     uint32_t band_start[9];      // first scan position of each significance band
     uint64_t t_lo, t_hi;         // box atoms the inverse transform launch covers
+    uint32_t box_table;          // 1: atoms[] is indexed by box atom (staged decode), 0: by LOD raster
 };
+
+__host__ __device__ inline uint64_t job_atom(const DecodeJob &J, uint64_t t, uint32_t az, uint32_t ay,
+                                             uint32_t ax) {
+    return J.box_table ? t : ((uint64_t)az * J.acy + ay) * J.acx + ax;
+}
 
 // Optional per-stage events: ev[0] before the list placement, ev[1] before the
 // range decoder, ev[2] before the inverse transform, ev[3] after it.

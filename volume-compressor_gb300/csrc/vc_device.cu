@@ -69,6 +69,7 @@ static void ctx_free(void *p) {
     for (int i = 0; i < VCD_NBUF; ++i)
         if (c->buf[i]) cudaFree(c->buf[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->stage_host) cudaFreeHost(c->stage_host);
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     if (c->copy_stream) {
         for (int i = 0; i < 16; ++i) cudaEventDestroy(c->chunk_ev[i]);
@@ -219,10 +220,10 @@ extern "C" void vcd_free_archive(vcd_archive *d) {
 }
 
 // ---------------------------------------------------------------- decode
-extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *out_dev, uint8_t *out_host,
-                                 size_t out_bytes) {
-    vcd_ctx *c = vcd_thread_ctx();
-    if (!c) return 4;
+// One box decode from device bytes `arc` and atom table `atoms` (LOD raster, or
+// box order when box_table). last_ms spans from `t0` (or the first stage event).
+static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uint32_t box_table, const vcd_dq *dq,
+                      const vcd_region *r, uint8_t *out_dev, uint8_t *out_host, size_t out_bytes, cudaEvent_t t0) {
     cudaError_t e;
     const uint64_t n = r->n_atoms;
     const uint64_t box_atoms = (uint64_t)r->bnx * r->bny * r->bnz;
@@ -247,8 +248,9 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
         vcd_set_error("decode output", e);
         return vcd_status_of(e);
     }
-    J.arc = d->arc;
-    J.atoms = d->atoms + r->atom_base;
+    J.arc = arc;
+    J.atoms = atoms;
+    J.box_table = box_table;
     J.acx = r->acx; J.acy = r->acy;
     J.bax = r->bax; J.bay = r->bay; J.baz = r->baz; J.bnx = r->bnx; J.bny = r->bny;
     J.n_atoms = n;
@@ -258,7 +260,7 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
     J.ent = (uint32_t *)p_ent;
     J.ent_off = (uint64_t *)p_off;
     J.cnt = (uint32_t *)p_cnt;
-    J.dq = d->dq + r->lod;
+    J.dq = dq;
     J.alt_mask = g_dev.tables->alt_mask;
     J.scan = g_dev.tables->scan;
     J.err = (uint32_t *)p_err;
@@ -327,7 +329,7 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
         vcd_set_error("decode kernels", e);
         return vcd_status_of(e);
     }
-    c->last_ms = vcd_elapsed(ev.ev[0], ev.ev[3]);
+    c->last_ms = vcd_elapsed(t0 ? t0 : ev.ev[0], ev.ev[3]);
     if (vcd_prof_on()) {
         const uint64_t nnz = ctl_h[1];
         vcd_prof_add("decode_place", vcd_elapsed(ev.ev[0], ev.ev[1]), n ? 2 : 0, 24 * n, 8 * n, n);
@@ -369,4 +371,91 @@ extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *o
     }
     free(tmp);
     return status;
+}
+
+extern "C" int vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *out_dev, uint8_t *out_host,
+                                 size_t out_bytes) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    return decode_job(c, d->arc, d->atoms + r->atom_base, 0, d->dq + r->lod, r, out_dev, out_host, out_bytes, NULL);
+}
+
+// ---------------------------------------------------------------- streamed decode
+
+extern "C" int vcd_upload_dq(vcd_archive **out, const vcd_dq *dq, int nlod) {
+    vcd_archive *d = (vcd_archive *)calloc(1, sizeof(vcd_archive));
+    if (!d) return 3;
+    cudaError_t e;
+    if ((e = cudaMalloc(&d->dq, nlod * sizeof(vcd_dq))) != cudaSuccess ||
+        (e = cudaMemcpy(d->dq, dq, nlod * sizeof(vcd_dq), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        vcd_set_error("dequantisation tables", e);
+        vcd_free_archive(d);
+        return vcd_status_of(e);
+    }
+    d->nlod = nlod;
+    *out = d;
+    return 0;
+}
+
+extern "C" int vcd_stage_reserve(size_t bytes, uint8_t **host) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    c->stage_started = 0;
+    cudaError_t e;
+    // uploads of an earlier call that ended early may still read the staging
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+        vcd_set_error("staging", e);
+        return vcd_status_of(e);
+    }
+    if (c->stage_cap < bytes) {
+        if (c->stage_host) cudaFreeHost(c->stage_host);
+        c->stage_host = NULL;
+        c->stage_cap = 0;
+        const size_t want = bytes + bytes / 4;
+        if ((e = cudaMallocHost(&c->stage_host, want)) != cudaSuccess) {
+            c->stage_host = NULL;
+            vcd_set_error("staging", e);
+            return vcd_status_of(e);
+        }
+        c->stage_cap = want;
+    }
+    void *dev;
+    if ((e = vcd_scratch(c, VCD_BUF_STG, bytes + 16, &dev)) != cudaSuccess) {
+        vcd_set_error("staging", e);
+        return vcd_status_of(e);
+    }
+    *host = c->stage_host;
+    return 0;
+}
+
+extern "C" int vcd_stage_push(size_t off, size_t bytes) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c || !c->stage_host || off + bytes > c->stage_cap || off + bytes + 16 > c->cap[VCD_BUF_STG]) return 4;
+    if (!c->stage_started) {
+        cudaEventRecord(c->ev[4], c->stream);
+        c->stage_started = 1;
+    }
+    if (!bytes) return 0;
+    cudaError_t e = cudaMemcpyAsync((uint8_t *)c->buf[VCD_BUF_STG] + off, c->stage_host + off, bytes,
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) {
+        vcd_set_error("staging upload", e);
+        return vcd_status_of(e);
+    }
+    return 0;
+}
+
+extern "C" int vcd_decode_staged(vcd_archive *d, const vcd_region *r, size_t table_off, size_t arena_off,
+                                 size_t arena_bytes, uint8_t *out_dev, uint8_t *out_host, size_t out_bytes) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    if (arena_off + arena_bytes + 16 > c->cap[VCD_BUF_STG] || table_off + r->n_atoms * sizeof(vcd_atom) > arena_off)
+        return 4;
+    uint8_t *stg = (uint8_t *)c->buf[VCD_BUF_STG];
+    // 16 zero bytes after the last payload, as after a resident archive
+    cudaMemsetAsync(stg + arena_off + arena_bytes, 0, 16, c->stream);
+    const int rc = decode_job(c, stg + arena_off, (const vcd_atom *)(stg + table_off), 1, d->dq + r->lod, r, out_dev,
+                              out_host, out_bytes, c->stage_started ? c->ev[4] : NULL);
+    c->stage_started = 0;
+    return rc;
 }

@@ -143,8 +143,12 @@ void vch_tables(vcd_tables *t) {
 // Reader (src/vc/vc.c:1250-1555)
 // ---------------------------------------------------------------------------
 struct vc_archive {
-    const uint8_t *buf;
+    const uint8_t *buf;     // flat archive (vc_open), or the pulled copy of a resident streaming one
     size_t len;
+    vc_read_fn read;        // streaming byte source (vc_open_streaming), else NULL
+    void *ud;
+    uint8_t *own;           // buf when pulled through read
+    uint8_t hdr[FILE_HDR];
     vc_dims d0;
     int nlod, version;
     uint64_t l1_off, l1_cap, dir_off, region_prefix[VC_NLOD + 1];
@@ -155,7 +159,17 @@ struct vc_archive {
     vcd_atom *atoms;        // all LODs, LOD-major, raster (az, ay, ax) within a LOD
     uint64_t lod_base[VC_NLOD + 1];
     vcd_archive *dev;
+    vcd_archive *sdev;      // streamed decode: dequantisation tables only
 };
+
+// Bytes [off, off + len) of the archive: a pointer into a flat archive's
+// buffer, or tmp filled by the read callback; NULL when the range lies outside
+// a flat archive or the read fails (src/vc/vc.c:1262-1267).
+static const uint8_t *at(const vc_archive *a, uint64_t off, uint32_t len, uint8_t *tmp) {
+    const uint8_t *buf = __atomic_load_n(&a->buf, __ATOMIC_ACQUIRE);
+    if (buf) return (off > a->len || len > a->len - off) ? NULL : buf + off;
+    return a->read(a->ud, off, len, tmp) == VC_OK ? tmp : NULL;
+}
 
 static int parse_header(vc_archive *a, const uint8_t *h, uint64_t len) {   // src/vc/vc.c:1285-1314
     if (rd32(h + 0) != MAGIC || rd32(h + 8) != 32 || rd32(h + 16) != R_ATOMS) return -1;
@@ -194,13 +208,36 @@ VC_API vc_archive *vc_open(const uint8_t *archive, size_t len) {
     if (!a) return NULL;
     a->buf = archive;
     if (parse_header(a, archive, len) != 0) { free(a); return NULL; }
+    memcpy(a->hdr, archive, FILE_HDR);
     pthread_mutex_init(&a->mu, NULL);
     return a;
+}
+
+VC_API vc_archive *vc_open_streaming(vc_read_fn read, void *ud, uint64_t total_len) {   // src/vc/vc.c:1329-1338
+    if (!read || total_len < FILE_HDR) return NULL;
+    vc_archive *a = (vc_archive *)calloc(1, sizeof *a);
+    if (!a) return NULL;
+    if (read(ud, 0, FILE_HDR, a->hdr) != VC_OK || parse_header(a, a->hdr, total_len) != 0) { free(a); return NULL; }
+    a->read = read;
+    a->ud = ud;
+    pthread_mutex_init(&a->mu, NULL);
+    return a;
+}
+
+VC_API vc_status vcg_memory_read(void *ud, uint64_t off, uint32_t len, uint8_t *dst) {
+    vcg_memory_source *m = (vcg_memory_source *)ud;
+    if (!m || !dst || off > m->len || len > m->len - off) return VC_ERR_FORMAT;
+    memcpy(dst, m->buf + off, len);
+    __atomic_fetch_add(&m->reads, 1, __ATOMIC_RELAXED);
+    __atomic_fetch_add(&m->bytes, len, __ATOMIC_RELAXED);
+    return VC_OK;
 }
 
 VC_API void vc_close(vc_archive *a) {
     if (!a) return;
     if (a->dev) vcd_free_archive(a->dev);
+    if (a->sdev) vcd_free_archive(a->sdev);
+    free(a->own);
     free(a->atoms);
     pthread_mutex_destroy(&a->mu);
     free(a);
@@ -219,13 +256,15 @@ VC_API vc_status vc_lod_dims(const vc_archive *a, int lod, vc_dims *out) {
 // forever on a full table without the key; src/vc/vc.c:1349-1360).
 static uint64_t region_block(const vc_archive *a, int lod, uint32_t rz, uint32_t ry, uint32_t rx) {
     uint64_t blk;
+    uint8_t tmp[16];
     if (a->version == 2) {
         uint32_t nrz, nry, nrx;
         region_grid(a->d0, lod, &nrz, &nry, &nrx);
         if (rz >= nrz || ry >= nry || rx >= nrx) return 0;
         uint64_t ri = a->region_prefix[lod] + ((uint64_t)rz * nry + ry) * nrx + rx;
         if (ri >= a->region_prefix[a->nlod]) return 0;
-        const uint8_t *e = a->buf + a->dir_off + ri * 16;
+        const uint8_t *e = at(a, a->dir_off + ri * 16, 16, tmp);
+        if (!e) return 0;
         uint32_t fl = rd32(e + 12);
         if (fl == 0) return 0;
         if (fl == 1) return ZERO_REGION;
@@ -234,7 +273,8 @@ static uint64_t region_block(const vc_archive *a, int lod, uint32_t rz, uint32_t
         uint64_t key = vch_region_key(lod, rz, ry, rx), mask = a->l1_cap - 1, i = vch_mix64(key) & mask;
         for (uint64_t step = 0;; ++step) {
             if (step >= a->l1_cap) return 0;
-            const uint8_t *e = a->buf + a->l1_off + i * 16;
+            const uint8_t *e = at(a, a->l1_off + i * 16, 16, tmp);
+            if (!e) return 0;
             uint64_t bref = rd64(e + 8);
             if (!bref) return 0;
             if (rd64(e) == key) { blk = bref; break; }
@@ -251,7 +291,9 @@ static int slot_of(const vc_archive *a, uint64_t blk, uint32_t az, uint32_t ay, 
                    uint64_t *off, uint32_t *len, uint8_t *dc) {
     if (blk == 0) return 0;
     if (blk == ZERO_REGION) return 2;
-    const uint8_t *s = a->buf + blk + ((((uint64_t)(az & 31) * 32 + (ay & 31)) * 32 + (ax & 31)) * 16);
+    uint8_t tmp[16];
+    const uint8_t *s = at(a, blk + ((((uint64_t)(az & 31) * 32 + (ay & 31)) * 32 + (ax & 31)) * 16), 16, tmp);
+    if (!s) return 0;
     uint8_t fl = s[12];
     if (fl == 1) { *off = rd64(s); *len = rd32(s + 8); *dc = s[13]; }
     return fl;
@@ -290,13 +332,34 @@ VC_API vc_cover vc_region_blob_range(const vc_archive *a, int lod, uint32_t rz, 
     if (rz >= nrz || ry >= nry || rx >= nrx) return VC_ABSENT;
     uint64_t ri = a->region_prefix[lod] + ((uint64_t)rz * nry + ry) * nrx + rx;
     if (ri >= a->region_prefix[a->nlod]) return VC_ABSENT;
-    const uint8_t *e = a->buf + a->dir_off + ri * 16;
+    uint8_t tmp[16];
+    const uint8_t *e = at(a, a->dir_off + ri * 16, 16, tmp);
+    if (!e) return VC_ABSENT;
     uint32_t fl = rd32(e + 12);
     if (fl == 1) return VC_KNOWN_ZERO;
     if (fl != 2) return VC_ABSENT;
     if (off) *off = rd64(e);
     if (len) *len = rd32(e + 8);
     return VC_PRESENT;
+}
+
+// A streaming archive pulled whole through its read callback into a host copy
+// (64 MiB per call); on a failed read it stays streaming.
+static int pull_whole(vc_archive *a) {
+    uint8_t *b = (uint8_t *)malloc(a->len ? a->len : 1);
+    if (!b) return -1;
+    for (uint64_t off = 0; off < a->len;) {
+        const uint32_t n = a->len - off > (64u << 20) ? (64u << 20) : (uint32_t)(a->len - off);
+        if (a->read(a->ud, off, n, b + off) != VC_OK) {
+            report("streaming archive: read of %u bytes at %llu failed", n, (unsigned long long)off);
+            free(b);
+            return -1;
+        }
+        off += n;
+    }
+    a->own = b;
+    __atomic_store_n(&a->buf, (const uint8_t *)b, __ATOMIC_RELEASE);
+    return 0;
 }
 
 // Resolve every atom of every LOD once, validate payload ranges, and move the
@@ -306,6 +369,7 @@ static int make_resident(vc_archive *a) {
     if (a->resident) { int r = a->resident; pthread_mutex_unlock(&a->mu); return r > 0 ? 0 : -1; }
     int rc = -1;
     if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); goto done; }
+    if (!a->buf && pull_whole(a) != 0) { pthread_mutex_unlock(&a->mu); return -1; }
     uint64_t total = 0;
     for (int l = 0; l < a->nlod; ++l) {
         vc_dims d = lod_dims_of(a->d0, l);
@@ -360,9 +424,238 @@ static inline uint64_t entry_cap(const vcd_atom *t) {
     return c > VCD_MAX_ENTRIES ? VCD_MAX_ENTRIES : c;
 }
 
+// ---------------------------------------------------------------------------
+// Streamed decode (vc_open_streaming, src/vc/vc.c:1262-1280, 1329-1338): the
+// box's index entries, slots and payloads come from the read callback. The
+// slots of one box row inside one region are read in one call, and payloads
+// that lie back to back in the file in one call per run of at most RUN_MAX
+// bytes; a call that fails is repeated slot by slot / payload by payload, so
+// every slot and payload gets the outcome its own read would give. Payloads
+// are packed into pinned staging behind a box-local atom table, uploaded piece
+// by piece while the next pieces are read, and decoded on the device.
+// ---------------------------------------------------------------------------
+#define STREAM_PAYLOAD_MAX (32768u * 4u + 64u)   // the reference's streaming payload scratch (src/vc/vc.c:1277)
+#define RUN_MAX (4u << 20)
+#define PIECE_MIN (16ull << 10)   // uploads: 1/16 of the payload, within [PIECE_MIN, PIECE_MAX]
+#define PIECE_MAX (16ull << 20)
+
+static int g_stream_threads = 1;
+VC_API int vcg_set_stream_threads(int n) {
+    if (n < 1) n = 1;
+    if (n > 64) n = 64;
+    return __atomic_exchange_n(&g_stream_threads, n, __ATOMIC_RELAXED);
+}
+
+typedef struct {
+    uint64_t src, dst;      // archive offset, staging offset (relative to the payload area)
+    uint32_t len, p0, p1;   // bytes; present atoms pidx[p0 .. p1)
+} stream_run;
+
+typedef struct {
+    const vc_archive *a;
+    const stream_run *runs;
+    const uint64_t *pidx, *psrc;   // per present atom: box index, archive offset
+    const vcd_atom *tab;
+    uint8_t *arena;
+    const uint32_t *piece_run;     // piece k = runs[piece_run[k] .. piece_run[k+1])
+    uint32_t n_pieces;
+    uint32_t next;                 // next piece to take (workers)
+    uint8_t *done;                 // per piece
+    uint64_t fail;                 // lowest box index whose payload read failed
+    pthread_mutex_t mu;
+    pthread_cond_t cv;
+} stream_fetch;
+
+static void fetch_piece(stream_fetch *f, uint32_t k) {
+    uint64_t fail = UINT64_MAX;
+    for (uint32_t r = f->piece_run[k]; r < f->piece_run[k + 1] && fail == UINT64_MAX; ++r) {
+        const stream_run *R = &f->runs[r];
+        if (f->a->read(f->a->ud, R->src, R->len, f->arena + R->dst) == VC_OK) continue;
+        for (uint32_t p = R->p0; p < R->p1; ++p) {
+            const vcd_atom *t = &f->tab[f->pidx[p]];
+            if (f->a->read(f->a->ud, f->psrc[p], t->len, f->arena + t->off) != VC_OK) { fail = f->pidx[p]; break; }
+        }
+    }
+    pthread_mutex_lock(&f->mu);
+    if (fail < f->fail) f->fail = fail;
+    f->done[k] = 1;
+    pthread_cond_broadcast(&f->cv);
+    pthread_mutex_unlock(&f->mu);
+}
+
+static void *fetch_worker(void *p) {
+    stream_fetch *f = (stream_fetch *)p;
+    for (;;) {
+        const uint32_t k = __atomic_fetch_add(&f->next, 1, __ATOMIC_RELAXED);
+        if (k >= f->n_pieces) return NULL;
+        fetch_piece(f, k);
+    }
+}
+
+static int stream_device(vc_archive *a) {   // dequantisation tables on the device, once
+    pthread_mutex_lock(&a->mu);
+    int rc = 0;
+    if (!a->sdev) {
+        vcd_dq dq[VC_NLOD];
+        for (int l = 0; l < a->nlod; ++l) vch_dq_consts(a->base_q[l], &dq[l]);
+        if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); rc = -1; }
+        else if (vcd_upload_dq(&a->sdev, dq, a->nlod) != 0) { report("%s", vcd_last_error()); rc = -1; }
+    }
+    pthread_mutex_unlock(&a->mu);
+    return rc;
+}
+
+static vc_status decode_box_streamed(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev) {
+    if (stream_device(a) != 0) return VC_ERR_IO;
+    const vc_dims d = lod_dims_of(a->d0, lod);
+    vcd_region r;
+    memset(&r, 0, sizeof r);
+    r.lod = lod;
+    r.acx = (d.nx + 31) / 32; r.acy = (d.ny + 31) / 32; r.acz = (d.nz + 31) / 32;
+    r.x0 = b.x0; r.y0 = b.y0; r.z0 = b.z0; r.x1 = b.x1; r.y1 = b.y1; r.z1 = b.z1;
+    r.bax = b.x0 / 32; r.bay = b.y0 / 32; r.baz = b.z0 / 32;
+    r.bnx = (b.x1 - 1) / 32 - r.bax + 1; r.bny = (b.y1 - 1) / 32 - r.bay + 1; r.bnz = (b.z1 - 1) / 32 - r.baz + 1;
+    const uint64_t n = (uint64_t)r.bnx * r.bny * r.bnz;
+    const size_t out_bytes = (size_t)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
+    // regions the box touches: their blocks, resolved once
+    const uint32_t rx0 = r.bax / 32, ry0 = r.bay / 32, rz0 = r.baz / 32;
+    const uint32_t nrx = (r.bax + r.bnx - 1) / 32 - rx0 + 1, nry = (r.bay + r.bny - 1) / 32 - ry0 + 1,
+                   nrz = (r.baz + r.bnz - 1) / 32 - rz0 + 1;
+    uint64_t *blk = (uint64_t *)malloc((size_t)nrx * nry * nrz * sizeof(uint64_t));
+    vcd_atom *tab = (vcd_atom *)malloc(n * sizeof(vcd_atom));
+    uint64_t *psrc = (uint64_t *)malloc(n * sizeof(uint64_t)), *pidx = (uint64_t *)malloc(n * sizeof(uint64_t));
+    stream_run *runs = (stream_run *)malloc((n + 1) * sizeof(stream_run));
+    uint32_t *piece_run = NULL;
+    uint8_t *done = NULL;
+    vc_status st = VC_OK;
+    if (!blk || !tab || !psrc || !pidx || !runs) { st = VC_ERR_OOM; goto out; }
+    for (uint32_t z = 0; z < nrz; ++z)
+        for (uint32_t y = 0; y < nry; ++y)
+            for (uint32_t x = 0; x < nrx; ++x)
+                blk[((uint64_t)z * nry + y) * nrx + x] = region_block(a, lod, rz0 + z, ry0 + y, rx0 + x);
+    // slots, box order; the first bad atom ends the box (src/vc/vc.c:1413-1416)
+    uint64_t nb = n, np = 0, pay = 0;
+    for (uint32_t z = 0; z < r.bnz && nb == n; ++z)
+        for (uint32_t y = 0; y < r.bny && nb == n; ++y) {
+            const uint32_t az = r.baz + z, ay = r.bay + y;
+            for (uint32_t x = 0; x < r.bnx && nb == n;) {
+                const uint32_t ax = r.bax + x, seg = (32 - (ax & 31)) < (r.bnx - x) ? 32 - (ax & 31) : r.bnx - x;
+                const uint64_t t0 = ((uint64_t)z * r.bny + y) * r.bnx + x;
+                const uint64_t bk = blk[((uint64_t)(az / 32 - rz0) * nry + (ay / 32 - ry0)) * nrx + (ax / 32 - rx0)];
+                uint8_t row[32 * 16];
+                const uint8_t *sl = NULL;
+                if (bk != 0 && bk != ZERO_REGION)
+                    sl = at(a, bk + ((((uint64_t)(az & 31) * 32 + (ay & 31)) * 32 + (ax & 31)) * 16), seg * 16, row);
+                for (uint32_t i = 0; i < seg; ++i) {
+                    vcd_atom *t = &tab[t0 + i];
+                    memset(t, 0, sizeof *t);
+                    uint64_t off = 0;
+                    uint32_t len = 0;
+                    uint8_t dc = 0;
+                    int fl;
+                    if (sl) {
+                        const uint8_t *s8 = sl + i * 16;
+                        fl = s8[12];
+                        if (fl == 1) { off = rd64(s8); len = rd32(s8 + 8); dc = s8[13]; }
+                    } else {
+                        fl = slot_of(a, bk, az, ay, ax + i, &off, &len, &dc);
+                    }
+                    if (fl != 1) { t->kind = VCD_EMPTY; continue; }
+                    if (off == NO_OFFSET || len < 1 || off > a->len || len > a->len - off || len > STREAM_PAYLOAD_MAX) {
+                        nb = t0 + i;
+                        break;
+                    }
+                    t->kind = VCD_PRESENT; t->off = pay; t->len = len; t->dc = dc;
+                    pidx[np] = t0 + i;
+                    psrc[np++] = off;
+                    pay += len;
+                }
+                x += seg;
+            }
+        }
+    // runs of payloads that follow one another in the file, grouped into pieces
+    uint32_t nr = 0;
+    for (uint64_t p = 0; p < np;) {
+        stream_run *R = &runs[nr++];
+        R->src = psrc[p]; R->dst = tab[pidx[p]].off; R->len = tab[pidx[p]].len; R->p0 = (uint32_t)p;
+        for (++p; p < np && psrc[p] == R->src + R->len && R->len + tab[pidx[p]].len <= RUN_MAX; ++p)
+            R->len += tab[pidx[p]].len;
+        R->p1 = (uint32_t)p;
+    }
+    const uint64_t piece = pay / 16 < PIECE_MIN ? PIECE_MIN : pay / 16 > PIECE_MAX ? PIECE_MAX : pay / 16;
+    const uint32_t max_pieces = (uint32_t)(pay / piece) + 2;
+    piece_run = (uint32_t *)malloc((max_pieces + 1) * sizeof(uint32_t));
+    done = (uint8_t *)calloc(max_pieces, 1);
+    if (!piece_run || !done) { st = VC_ERR_OOM; goto out; }
+    uint32_t npc = 0;
+    piece_run[0] = 0;
+    for (uint32_t i = 0; i < nr;) {
+        const uint64_t base = runs[i].dst;
+        while (i < nr && (runs[i].dst - base < piece || runs[i].dst == base)) ++i;
+        piece_run[++npc] = i;
+    }
+    // staging: [table (nb atoms)][pad to 256][payloads]
+    const size_t table_bytes = (size_t)nb * sizeof(vcd_atom), arena_off = (table_bytes + 255) & ~(size_t)255;
+    uint8_t *stage = NULL;
+    int e = vcd_stage_reserve(arena_off + pay, &stage);
+    if (e) { st = (vc_status)e; report("streamed decode: %s", vcd_last_error()); goto out; }
+    memcpy(stage, tab, table_bytes);
+    if ((e = vcd_stage_push(0, table_bytes)) != 0) { st = (vc_status)e; goto out; }
+    stream_fetch f;
+    memset(&f, 0, sizeof f);
+    f.a = a; f.runs = runs; f.pidx = pidx; f.psrc = psrc; f.tab = tab; f.arena = stage + arena_off;
+    f.piece_run = piece_run; f.n_pieces = npc; f.done = done; f.fail = UINT64_MAX;
+    pthread_mutex_init(&f.mu, NULL);
+    pthread_cond_init(&f.cv, NULL);
+    const int want = __atomic_load_n(&g_stream_threads, __ATOMIC_RELAXED);
+    const int nthr = npc > 1 && want > 1 ? (want < (int)npc ? want : (int)npc) : 0;
+    pthread_t th[64];
+    int started = 0;
+    for (; started < nthr; ++started)
+        if (pthread_create(&th[started], NULL, fetch_worker, &f) != 0) break;
+    for (uint32_t k = 0; k < npc && !e; ++k) {
+        if (!started) {
+            fetch_piece(&f, k);
+        } else {
+            pthread_mutex_lock(&f.mu);
+            while (!done[k]) pthread_cond_wait(&f.cv, &f.mu);
+            pthread_mutex_unlock(&f.mu);
+        }
+        const uint64_t lo = runs[piece_run[k]].dst;
+        const uint64_t hi = runs[piece_run[k + 1] - 1].dst + runs[piece_run[k + 1] - 1].len;
+        e = vcd_stage_push(arena_off + lo, hi - lo);
+    }
+    if (started) {
+        __atomic_store_n(&f.next, npc, __ATOMIC_RELAXED);   // no new pieces after an upload error
+        for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
+    }
+    pthread_cond_destroy(&f.cv);
+    pthread_mutex_destroy(&f.mu);
+    if (e) { st = (vc_status)e; report("streamed decode: %s", vcd_last_error()); goto out; }
+    if (f.fail < nb) nb = f.fail;
+    uint64_t cap = 0, bytes = 0, present = 0;
+    for (uint64_t p = 0; p < np && pidx[p] < nb; ++p) {
+        cap += entry_cap(&tab[pidx[p]]);
+        bytes += tab[pidx[p]].len;
+        ++present;
+    }
+    r.n_atoms = nb;
+    r.cap_total = cap;
+    r.payload_bytes = bytes;
+    r.present = present;
+    e = vcd_decode_staged(a->sdev, &r, 0, arena_off, pay, out_dev, out, out_bytes);
+    if (e && e != VC_ERR_FORMAT) report("streamed decode: %s", vcd_last_error());
+    st = (vc_status)e;
+    if (!e && nb < n) st = VC_ERR_FORMAT;
+out:
+    free(blk); free(tab); free(psrc); free(pidx); free(runs); free(piece_run); free(done);
+    return st;
+}
+
 // Shared by decode_region / decode_atom / decode_lod: out_dev (device) or out
 // (host) receives the box raster.
 static vc_status decode_box(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev) {
+    if (a->read && __atomic_load_n(&a->resident, __ATOMIC_ACQUIRE) != 1) return decode_box_streamed(a, lod, b, out, out_dev);
     if (make_resident(a) != 0) return VC_ERR_IO;
     vc_dims d = lod_dims_of(a->d0, lod);
     vcd_region r;
@@ -733,10 +1026,10 @@ VC_API vc_status vcg_repack_v2(vc_archive *a, uint8_t **out_archive, size_t *out
         memcpy(head, w, sizeof w);
         const uint32_t dims[3] = {a->d0.nx, a->d0.ny, a->d0.nz};
         memcpy(head + 24, dims, sizeof dims);
-        memcpy(head + 36, a->buf + 36, 4);   // target ratio
+        memcpy(head + 36, a->hdr + 36, 4);   // target ratio
         const uint64_t h64[3] = {dir_off, total_regions, cursor};
         memcpy(head + 40, h64, sizeof h64);
-        memcpy(head + 72, a->buf + 72, 4 * VC_NLOD);   // base_q per LOD
+        memcpy(head + 72, a->hdr + 72, 4 * VC_NLOD);   // base_q per LOD
         uint8_t *res = (uint8_t *)malloc(cursor);
         if (!res) {
             rc = VC_ERR_OOM;

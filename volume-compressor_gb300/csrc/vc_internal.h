@@ -98,6 +98,17 @@ void vcd_free_archive(vcd_archive *d);
 int  vcd_decode_region(vcd_archive *d, const vcd_region *r, uint8_t *out_dev, uint8_t *out_host,
                        size_t out_bytes);
 
+// Streamed decode (archives opened on a read callback). The archive's device
+// side holds only the dequantisation tables. Per call, the host fills a pinned
+// staging area: a box-local atom table (one vcd_atom per box atom, box order
+// z, y, x, offsets relative to the payload area) and the payloads packed after
+// it; uploads of finished pieces overlap the filling of the next.
+int  vcd_upload_dq(vcd_archive **out, const vcd_dq *dq /*nlod*/, int nlod);
+int  vcd_stage_reserve(size_t bytes, uint8_t **host);          // pinned staging of >= bytes
+int  vcd_stage_push(size_t off, size_t bytes);                 // async upload of [off, off+bytes)
+int  vcd_decode_staged(vcd_archive *d, const vcd_region *r, size_t table_off, size_t arena_off,
+                       size_t arena_bytes, uint8_t *out_dev, uint8_t *out_host, size_t out_bytes);
+
 // Batched decode. Outputs: reqs[i].out (device) when host_out is NULL, else
 // host_out[i] (the device layer stages through its own buffer). req_err[i] is
 // set to 1 for requests that met a malformed stream.

@@ -20,9 +20,10 @@ VC_ABSENT, VC_KNOWN_ZERO, VC_PRESENT = 0, 1, 2
 # Every symbol the public headers declare (checked by the CPU test suite).
 VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod", "vc_decode_atom",
               "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
-              "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook"]
+              "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook", "vc_open_streaming"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps", "vcg_dct_forward", "vcg_dct_inverse",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps",
+               "vcg_set_stream_threads", "vcg_memory_read", "vcg_dct_forward", "vcg_dct_inverse",
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
@@ -134,6 +135,9 @@ def lib():
         L.vc_encode.argtypes = [P, Dims, ctypes.c_float, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_size_t)]
         L.vc_open.restype = P
         L.vc_open.argtypes = [P, ctypes.c_size_t]
+        L.vc_open_streaming.restype = P
+        L.vc_open_streaming.argtypes = [P, P, ctypes.c_uint64]
+        L.vcg_set_stream_threads.argtypes = [ctypes.c_int]
         L.vc_close.argtypes = [P]
         L.vc_lod_dims.argtypes = [P, ctypes.c_int, ctypes.POINTER(Dims)]
         L.vc_decode_lod.argtypes = [P, ctypes.c_int, P, ctypes.POINTER(Dims)]
@@ -408,6 +412,51 @@ class Archive:
         o, l = ctypes.c_uint64(), ctypes.c_uint32()
         c = lib().vc_atom_payload_range(self.h, lod, az, ay, ax, ctypes.byref(o), ctypes.byref(l))
         return c, o.value, l.value
+
+
+READ_FN = ctypes.CFUNCTYPE(ctypes.c_int, P, ctypes.c_uint64, ctypes.c_uint32, P)
+
+
+class MemorySource(ctypes.Structure):
+    _fields_ = [("buf", P), ("len", ctypes.c_uint64), ("reads", ctypes.c_uint64), ("bytes", ctypes.c_uint64)]
+
+
+class StreamingArchive(Archive):
+    """vc_open_streaming. `source` is either the archive bytes, served by the
+    library's native vcg_memory_read, or a callable read(off, n) returning n
+    bytes (None or a short result fails the read). total_len defaults to the
+    length of the bytes."""
+
+    def __init__(self, source, total_len=None):
+        if callable(source):
+            def cb(ud, off, n, dst):
+                try:
+                    b = source(off, n)
+                except Exception:
+                    return VC_ERR_IO
+                if b is None or len(b) != n:
+                    return VC_ERR_FORMAT
+                ctypes.memmove(dst, bytes(b), n)
+                return VC_OK
+            self._cb = READ_FN(cb)
+            fn, ud = ctypes.cast(self._cb, P), None
+            self.src = None
+        else:
+            data = bytes(source)
+            self.buf = ctypes.create_string_buffer(data, len(data))
+            self.src = MemorySource(ctypes.addressof(self.buf), len(data), 0, 0)
+            fn, ud = ctypes.cast(lib().vcg_memory_read, P), ctypes.addressof(self.src)
+            if total_len is None:
+                total_len = len(data)
+        self.h = lib().vc_open_streaming(fn, ud, total_len)
+
+    def reads(self):
+        """(calls, bytes) served by the native memory source."""
+        return (self.src.reads, self.src.bytes) if self.src is not None else None
+
+
+def set_stream_threads(n):
+    return lib().vcg_set_stream_threads(n)
 
 
 # ---------------------------------------------------------------- synthetic volumes
