@@ -46,6 +46,7 @@ def args_parse():
     p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched-region measurement")
     p.add_argument("--no-served", action="store_true", help="skip the config-5 served-decode measurement")
     p.add_argument("--no-dct", action="store_true", help="skip the config-3 DCT-forms measurement")
+    p.add_argument("--no-ds", action="store_true", help="skip the exporter-downscale measurement")
     p.add_argument("--no-sweep", action="store_true", help="skip the config-2 target / LOD sweep")
     p.add_argument("--dct-size", type=int, default=1024, help="edge of the DCT-forms volume")
     p.add_argument("--dct-reps", type=int, default=3, help="timed calls per DCT form and direction (0: one call)")
@@ -486,6 +487,55 @@ def _equal_device(vc, a, b, nbytes, chunk=256 << 20):
     return True
 
 
+def downscale_bench(dvol, dims, peak, reps=5, slab=64):
+    """The exporter's 2x downscale (DS_BOX, and DS_CBOX at the exporter's
+    alpha 0.5) of the resident 1024^3 volume: the full cascade (levels 1..7)
+    and level 1 alone (the dominant launch: 1 GiB read, 128 MiB written), device
+    time, algorithmic GB/s and the fraction of the measured HBM copy rate.
+    Level 1 of a slab of `slab` planes is checked against the oracle, whose
+    time on that slab (one host thread) is the CPU leg."""
+    import numpy as np
+    import vc_gb300 as vc
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oraclelib
+    nx, ny, nz = dims
+    levels = 7
+    res = {}
+    for method, name, alpha in ((vc.DS_BOX, "box", 0.5), (vc.DS_CBOX, "cbox", 0.5)):
+        row = {}
+        for lv in (1, levels):
+            ms = []
+            for r in range(reps + 1):
+                s, bufs, dl = vc.downscale_pyramid(dvol, dims, method, alpha, lv)
+                assert s == 0, vc.last_error()
+                if r:
+                    ms.append(vc.last_call_ms())
+                if r < reps:
+                    for b in bufs:
+                        b.free()
+            m = statistics.median(ms)
+            dd = [tuple(dims)] + dl
+            alg = sum(dd[i][0] * dd[i][1] * dd[i][2] + dd[i + 1][0] * dd[i + 1][1] * dd[i + 1][2] for i in range(lv))
+            row[f"levels{lv}"] = {"ms": m, "algorithmic_bytes": alg, "GBps": alg / (m / 1e3) / 1e9,
+                                  "hbm_frac": alg / (m / 1e3) / 1e9 / peak}
+            if lv == 1:   # check a slab against the oracle (CPU leg)
+                ox, oy = dl[0][0], dl[0][1]
+                lvl1 = bufs[0].download(ox * oy * (slab // 2)).reshape(slab // 2, oy, ox)
+                host = np.empty((slab, ny, nx), np.uint8)
+                vc.lib().vcg_copy(host.ctypes.data, ctypes.c_void_p(dvol.ptr), host.nbytes)
+                t0 = time.perf_counter()
+                want = oraclelib.ds_downscale2x(host, method, alpha)
+                t_cpu = time.perf_counter() - t0
+                row["slab_matches_oracle"] = bool(np.array_equal(lvl1, want))
+                row["cpu_port_1thread_GBps"] = host.nbytes / t_cpu / 1e9
+            for b in bufs:
+                b.free()
+        res[name] = row
+    res["note"] = ("levels1 = one launch over the 1 GiB level 0; levels7 = the cascade to 8^3; "
+                   "algorithmic bytes = every level read once + its output written once")
+    return res
+
+
 def config3_dct(n=1024, reps=3, sample_atoms=256):
     """Whole-atom integer DCT of the 1024^3 volume, x = vox - dc per atom as the
     codec centres, forward and inverse, in both forms: butterfly (CUDA cores)
@@ -876,9 +926,11 @@ def gb300_arm(args, dist):
         if lod0_ok is None:
             lod0_ok = bool(np.array_equal(out.download(nbytes), ref_out.ravel()))
 
-    sweep = None
+    sweep = ds = None
     if dist.rank == 0 and not args.no_sweep:
         sweep = config2_sweep(dvol, dims, peak)
+    if dist.rank == 0 and not args.no_ds:
+        ds = downscale_bench(dvol, dims, peak)
     # the other workloads (rank 0): release the headline buffers first
     batched = dct = served = None
     if dist.rank == 0 and not (args.no_batched and args.no_dct and args.no_served):
@@ -928,6 +980,8 @@ def gb300_arm(args, dist):
         line["dct_forms"] = dct
     if sweep:
         line["config2_sweep"] = sweep
+    if ds:
+        line["exporter_downscale"] = ds
     print(json.dumps(line), flush=True)
 
 

@@ -118,6 +118,29 @@ vc_status vcg_encode_device(const uint8_t *vol_dev, vc_dims dims, float target_r
 vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
                        const float base_q[VC_NLOD], uint8_t **out_archive, size_t *out_len);
 
+// The exporter's 2x downscale (tools/downscale.h:29-93) on the GPU. Every
+// output voxel is a function of its own 2x2x2 cell; odd boundaries replicate
+// the edge voxel; output dims are (n + 1) / 2 per axis.
+//   VCG_DS_BOX   rounded mean, (sum + 4) >> 3 (the codec's own pyramid rule)
+//   VCG_DS_CBOX  the mean pushed by alpha toward the cell's voxel of largest
+//                deviation; the exporter's default, alpha 0.5
+// alpha must be finite; method anything else is VC_ERR_RANGE.
+#define VCG_DS_BOX 0
+#define VCG_DS_CBOX 1
+// One level: in and out both in device memory (on_device != 0) or both host.
+vc_status vcg_downscale2x(const uint8_t *in, int on_device, vc_dims dims, int method, float alpha, uint8_t *out,
+                          vc_dims *out_dims);
+// Levels 1..levels (at most 8) of the cascade of a device volume: out_dev[l-1]
+// receives level l, each level the downscale of the one before.
+vc_status vcg_downscale_pyramid(const uint8_t *vol_dev, vc_dims dims, int method, float alpha, int levels,
+                                uint8_t *const *out_dev);
+// vc_encode (base_q NULL: rate control) or vcg_encode_q (base_q given) with the
+// LOD pyramid built by the exporter's downscale instead of the codec's rule.
+// VCG_DS_BOX gives exactly the archive of vc_encode / vcg_encode_q.
+vc_status vcg_encode_ds(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
+                        const float base_q[VC_NLOD], int method, float alpha, uint8_t **out_archive,
+                        size_t *out_len);
+
 // Decode without allocating (no counterpart in the reference). For callers
 // that cannot let a library allocate device memory: applications that reserve
 // the whole GPU for their own pool up front, so a library cudaMalloc would

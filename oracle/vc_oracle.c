@@ -658,6 +658,71 @@ int orc_encode(const uint8_t *vol, orc_dims d, float target, int nthreads, uint8
 void orc_free(void *p) { free(p); }
 
 // ---------------------------------------------------------------------------
+// Exporter 2x downscale (tools/downscale.h:29-93), strictly within the 2x2x2
+// cell, odd boundaries edge-replicated. DS_BOX is the cell mean rounded half
+// up; DS_CBOX moves the mean toward the cell's voxel of largest deviation
+// (the first one in (dz, dy, dx) order on ties) by alpha. The deviations are
+// compared exactly as integers |8c - sum| (the reference's float differences
+// are exact). The push mean + alpha * (best - mean) is evaluated as the
+// reference's release build (gcc -O3 -ffast-math -ffp-contract=fast
+// -march=native) evaluates it: one fused multiply-add, except in the 8-lane
+// vector body of the nz == 2 fast path (tools/downscale.h:62-79; the first
+// 8 * floor(ox / 8) outputs of each row), where it multiplies and adds
+// separately. Pinned against that build cell by cell.
+// ---------------------------------------------------------------------------
+static int g_ds_fused = 1;
+void orc_ds_set_fused(int fused) { g_ds_fused = fused; }
+
+static uint8_t ds_cell_rule(const uint8_t *c8, int method, float alpha, int fused) {
+    uint32_t sum = 0;
+    for (int i = 0; i < 8; ++i) sum += c8[i];
+    if (sum == 0) return 0;
+    if (method == 0) return (uint8_t)((sum + 4) >> 3);
+    int best = c8[0], bestdev = -1;
+    for (int i = 0; i < 8; ++i) {
+        int d = 8 * (int)c8[i] - (int)sum;
+        if (d < 0) d = -d;
+        if (d > bestdev) { bestdev = d; best = c8[i]; }
+    }
+    const float mean = (float)sum * 0.125f, dlt = (float)best - mean;
+    const float v = fused ? fmaf(alpha, dlt, mean) : mean + alpha * dlt;
+    if (v < 0.0f) return 0;
+    if (v > 255.0f) return 255;
+    return (uint8_t)(v + 0.5f);
+}
+
+uint8_t orc_ds_cell(const uint8_t *c8, int method, float alpha) {   // :38-46
+    return ds_cell_rule(c8, method, alpha, g_ds_fused);
+}
+
+void orc_ds_downscale2x(const uint8_t *in, orc_dims d, int method, float alpha, uint8_t *out, orc_dims *od) {   // :48-93
+    orc_dims o = {(d.nx + 1) / 2, (d.ny + 1) / 2, (d.nz + 1) / 2};
+    if (o.nx < 1) o.nx = 1;
+    if (o.ny < 1) o.ny = 1;
+    if (o.nz < 1) o.nz = 1;
+    if (od) *od = o;
+    const int fast = d.nz == 2 && d.nx % 2 == 0 && d.ny % 2 == 0;   // :62
+    const uint32_t vec_end = fast ? o.nx & ~7u : 0;
+    for (uint32_t z = 0; z < o.nz; ++z)
+        for (uint32_t y = 0; y < o.ny; ++y)
+            for (uint32_t x = 0; x < o.nx; ++x) {
+                uint8_t c8[8];
+                int n = 0;
+                for (uint32_t dz = 0; dz < 2; ++dz)
+                    for (uint32_t dy = 0; dy < 2; ++dy)
+                        for (uint32_t dx = 0; dx < 2; ++dx) {
+                            uint32_t z2 = 2 * z + dz, y2 = 2 * y + dy, x2 = 2 * x + dx;
+                            if (z2 >= d.nz) z2 = d.nz - 1;
+                            if (y2 >= d.ny) y2 = d.ny - 1;
+                            if (x2 >= d.nx) x2 = d.nx - 1;
+                            c8[n++] = in[((size_t)z2 * d.ny + y2) * d.nx + x2];
+                        }
+                out[((size_t)z * o.ny + y) * o.nx + x] = ds_cell_rule(c8, method, alpha, x >= vec_end);
+            }
+}
+
+
+// ---------------------------------------------------------------------------
 // Reader (:1247-1555)
 // ---------------------------------------------------------------------------
 struct orc_archive {

@@ -43,6 +43,10 @@ int      orc_decode_atom_payload(const uint8_t *pay, uint32_t len, float base_q,
 
 // ---- pyramid (src/vc/vc.c:1562-1577)
 void     orc_downsample2x(const uint8_t *in, orc_dims d, uint8_t *out);
+// exporter downscale (tools/downscale.h): method 0 = DS_BOX, 1 = DS_CBOX
+uint8_t  orc_ds_cell(const uint8_t *c8, int method, float alpha);
+void     orc_ds_downscale2x(const uint8_t *in, orc_dims d, int method, float alpha, uint8_t *out, orc_dims *od);
+void     orc_ds_set_fused(int fused);   // CBOX push as one fma (default) or multiply + add
 int      orc_nlod(orc_dims d0);
 orc_dims orc_lod_dims_of(orc_dims d0, int lod);
 

@@ -266,3 +266,45 @@ class RefStreamingArchive(RefArchive):
             return 0
         self._cb = READ_FN(cb)
         self.h = lib().vc_open_streaming(ctypes.cast(self._cb, ctypes.c_void_p), None, total_len)
+
+
+DS_SO = os.path.join(ROOT, "oracle", "_ref", "libdsref.so")
+_ds = None
+
+
+def ds_downscale2x(vol, method, alpha):
+    """The reference exporter's ds_downscale2x (tools/downscale.h) on a (nz, ny, nx) volume."""
+    global _ds
+    if _ds is None:
+        _ds = ctypes.CDLL(DS_SO)
+        _ds.dsref_downscale2x.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 3 + \
+                                         [ctypes.c_int, ctypes.c_float]
+        _ds.dsref_cell.restype = ctypes.c_uint
+        _ds.dsref_cell.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float]
+    vol = np.ascontiguousarray(vol, np.uint8)
+    nz, ny, nx = vol.shape
+    out = np.zeros(((nz + 1) // 2, (ny + 1) // 2, (nx + 1) // 2), np.uint8)
+    o = [ctypes.c_int() for _ in range(3)]
+    _ds.dsref_downscale2x(vol.ctypes.data, nx, ny, nz, out.ctypes.data, *[ctypes.byref(v) for v in o], method,
+                          ctypes.c_float(alpha))
+    assert (o[0].value, o[1].value, o[2].value) == (out.shape[2], out.shape[1], out.shape[0])
+    return out
+
+
+def ds_cell(c8, method, alpha):
+    ds_downscale2x(np.zeros((1, 1, 1), np.uint8), 0, 0.0)   # loads the library
+    c8 = np.ascontiguousarray(c8, np.uint8)
+    return _ds.dsref_cell(c8.ctypes.data, method, ctypes.c_float(alpha))
+
+
+def ds_encode(vol, target, method, alpha, threads=8):
+    """vc_encode with the exporter's pyramid, composed from reference calls:
+    levels by ds_downscale2x, q0 by the present-atom bisection on LOD 0, the
+    writer in canonical order. Returns (bytes, q0, levels)."""
+    nz, ny, nx = vol.shape
+    lods = [vol]
+    for _ in range(1, nlod_of(nx, ny, nz)):
+        lods.append(ds_downscale2x(lods[-1], method, alpha))
+    q0, _, _ = rate_control(vol, target, threads)
+    return write_archive(lods, (nx, ny, nz), target, lod_qs(q0, len(lods))), q0, lods

@@ -60,6 +60,10 @@ def lib():
         L.orc_open.restype = P
         L.orc_open.argtypes = [P, ctypes.c_size_t]
         L.orc_open_streaming.restype = P
+        L.orc_ds_cell.restype = ctypes.c_uint8
+        L.orc_ds_cell.argtypes = [P, ctypes.c_int, ctypes.c_float]
+        L.orc_ds_downscale2x.argtypes = [P, Dims, ctypes.c_int, ctypes.c_float, P, ctypes.POINTER(Dims)]
+        L.orc_ds_set_fused.argtypes = [ctypes.c_int]
         L.orc_open_streaming.argtypes = [P, P, ctypes.c_uint64]
         L.orc_close.argtypes = [P]
         L.orc_lod_dims.argtypes = [P, ctypes.c_int, ctypes.POINTER(Dims)]
@@ -198,3 +202,11 @@ class StreamingArchive(Archive):
         self.h = lib().orc_open_streaming(ctypes.cast(self._cb, P), None, total_len)
 
 
+def ds_downscale2x(vol, method, alpha):
+    """The oracle's exporter downscale of a (nz, ny, nx) volume."""
+    vol = np.ascontiguousarray(vol, np.uint8)
+    nz, ny, nx = vol.shape
+    out = np.zeros(((nz + 1) // 2, (ny + 1) // 2, (nx + 1) // 2), np.uint8)
+    od = Dims()
+    lib().orc_ds_downscale2x(ptr(vol), Dims(nx, ny, nz), method, ctypes.c_float(alpha), ptr(out), ctypes.byref(od))
+    return out

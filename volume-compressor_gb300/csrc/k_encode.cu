@@ -1,7 +1,5 @@
 // Encode kernels.
 //
-//   k_downsample  LOD k -> k+1: integer mean of the in-bounds 2x2x2 children,
-//                 (acc + n/2) / n (src/vc/vc.c:1562-1577)
 //   k_fwd         one CTA per atom: gather (zero padding outside the volume),
 //                 sum -> zero flag + dc (src/vc/vc.c:599-604), forward DCT-32
 //                 passes x, y per z-slab then z per column (src/vc/vc.c:212-218),
@@ -25,23 +23,6 @@ namespace vcg {
 
 constexpr int kFwdThreads = 256;
 constexpr size_t kFwdSmem = 32768 * sizeof(int32_t) + 32768 * sizeof(int16_t);
-
-__global__ void k_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out) {
-    const uint32_t ox = (nx + 1) / 2, oy = (ny + 1) / 2, oz = (nz + 1) / 2;
-    const uint64_t n = (uint64_t)ox * oy * oz;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t x = (uint32_t)(i % ox), y = (uint32_t)((i / ox) % oy), z = (uint32_t)(i / ((uint64_t)ox * oy));
-        uint32_t acc = 0, cnt = 0;
-        for (uint32_t zz = 2 * z; zz < 2 * z + 2 && zz < nz; ++zz)
-            for (uint32_t yy = 2 * y; yy < 2 * y + 2 && yy < ny; ++yy) {
-                const uint8_t *row = in + ((uint64_t)zz * ny + yy) * nx;
-                acc += row[2 * x];
-                ++cnt;
-                if (2 * x + 1 < nx) { acc += row[2 * x + 1]; ++cnt; }
-            }
-        out[i] = (uint8_t)((acc + cnt / 2) / cnt);
-    }
-}
 
 // 32 voxels of row (z, y) of atom (az, ay, ax), zero outside the volume, packed
 // little-endian into 8 words.
@@ -335,11 +316,6 @@ void enc_set_smem() {
         cudaFuncSetAttribute(k_quant_cached, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQuantSmem);
         done = true;
     }
-}
-
-void launch_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, int num_sms,
-                       cudaStream_t s) {
-    k_downsample<<<num_sms * 8, 256, 0, s>>>(in, nx, ny, nz, out);
 }
 
 void launch_quant_cached(const FwdJob &J, int num_sms, cudaStream_t s) {

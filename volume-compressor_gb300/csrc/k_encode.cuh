@@ -83,8 +83,6 @@ struct PlaceJob {
     Layout lay;
 };
 
-void launch_downsample(const uint8_t *in, uint32_t nx, uint32_t ny, uint32_t nz, uint8_t *out, int num_sms,
-                       cudaStream_t s);
 void launch_fwd(const FwdJob &J, int num_sms, cudaStream_t s);
 // atoms that are all LOD0 with kept coefficients: quantise and compact only
 void launch_quant_cached(const FwdJob &J, int num_sms, cudaStream_t s);

@@ -8,6 +8,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "k_ds.cuh"
 #include "k_encode.cuh"
 #include "kernels.cuh"
 #include "vc_device.h"
@@ -123,13 +124,13 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     S.c = c;
     const int nlod = info->nlod;
     S.lay.nlod = nlod;
-    uint64_t nvox[8], pyr_bytes = 0, total_atoms = 0;
+    uint64_t nvox[8], pyr_bytes = 0, pyr_vox = 0, total_atoms = 0;
     uint32_t d[3] = {info->nx, info->ny, info->nz};
     for (int l = 0; l < nlod; ++l) {
         if (l) for (int k = 0; k < 3; ++k) d[k] = (d[k] + 1) / 2;
         memcpy(S.dims[l], d, sizeof d);
         nvox[l] = (uint64_t)d[0] * d[1] * d[2];
-        if (l) pyr_bytes += nvox[l];
+        if (l) pyr_bytes += (nvox[l] + 255) & ~255ull, pyr_vox += nvox[l];
         S.lay.acx[l] = (d[0] + 31) / 32; S.lay.acy[l] = (d[1] + 31) / 32; S.lay.acz[l] = (d[2] + 31) / 32;
         S.lay.base[l] = total_atoms;
         total_atoms += (uint64_t)S.lay.acx[l] * S.lay.acy[l] * S.lay.acz[l];
@@ -152,16 +153,17 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     {
         uint8_t *q = (uint8_t *)p;
         for (int l = 1; l < nlod; ++l) {
-            launch_downsample(S.lvol[l - 1], S.dims[l - 1][0], S.dims[l - 1][1], S.dims[l - 1][2], q, g_dev.num_sms, st);
+            launch_ds2x(S.lvol[l - 1], S.dims[l - 1][0], S.dims[l - 1][1], S.dims[l - 1][2], q, info->ds_method,
+                        info->ds_alpha, g_dev.num_sms, st);
             S.lvol[l] = q;
-            q += nvox[l];
+            q += (nvox[l] + 255) & ~255ull;   // 256-byte aligned levels (vector loads)
         }
     }
     if (prof && nlod > 1) {   // pyramid: every coarser voxel reads its (up to) 8 children
         cudaEventRecord(c->ev[5], st);
         cudaEventSynchronize(c->ev[5]);
-        vcd_prof_add("downsample", vcd_elapsed(c->ev[6], c->ev[5]), (uint64_t)(nlod - 1), nvox[0] + pyr_bytes - nvox[nlod - 1],
-                     pyr_bytes, pyr_bytes);
+        vcd_prof_add("downsample", vcd_elapsed(c->ev[6], c->ev[5]), (uint64_t)(nlod - 1), nvox[0] + pyr_vox - nvox[nlod - 1],
+                     pyr_vox, pyr_vox);
     }
     const uint64_t chunk = total_atoms < kChunk ? total_atoms : kChunk;
     CK(vcd_scratch(c, VCD_BUF_EENT, chunk * VCD_MAX_ENTRIES * 4 + 16, &p), "coefficient lists");

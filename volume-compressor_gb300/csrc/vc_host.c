@@ -887,11 +887,14 @@ static int nlod_for(vc_dims d0) {   // src/vc/vc.c:1001-1006
 }
 
 static vc_status encode_common(const uint8_t *vol, int on_device, vc_dims dims, float target,
-                               const float *fixed_q, uint8_t **out, size_t *out_len, float *q0) {
+                               const float *fixed_q, uint8_t **out, size_t *out_len, float *q0, int ds_method,
+                               float ds_alpha) {
     if (!vol || !out || !out_len || !dims_valid(dims) || !(target >= 1.0f)) return VC_ERR_RANGE;
     if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); return VC_ERR_IO; }
     vcd_encode_info info;
     memset(&info, 0, sizeof info);
+    info.ds_method = ds_method;
+    info.ds_alpha = ds_alpha;
     info.nx = dims.nx; info.ny = dims.ny; info.nz = dims.nz;
     info.target_ratio = target;
     info.nlod = nlod_for(dims);
@@ -918,18 +921,60 @@ static vc_status encode_common(const uint8_t *vol, int on_device, vc_dims dims, 
 
 VC_API vc_status vc_encode(const uint8_t *vol, vc_dims dims, float target_ratio, uint8_t **out_archive,
                            size_t *out_len) {
-    return encode_common(vol, 0, dims, target_ratio, NULL, out_archive, out_len, NULL);
+    return encode_common(vol, 0, dims, target_ratio, NULL, out_archive, out_len, NULL, VCG_DS_BOX, 0.0f);
 }
 
 VC_API vc_status vcg_encode_device(const uint8_t *vol_dev, vc_dims dims, float target_ratio,
                                    uint8_t **out_archive, size_t *out_len, float *q0) {
-    return encode_common(vol_dev, 1, dims, target_ratio, NULL, out_archive, out_len, q0);
+    return encode_common(vol_dev, 1, dims, target_ratio, NULL, out_archive, out_len, q0, VCG_DS_BOX, 0.0f);
 }
 
 VC_API vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
                               const float base_q[VC_NLOD], uint8_t **out_archive, size_t *out_len) {
     if (!base_q) return VC_ERR_RANGE;
-    return encode_common(vol, vol_on_device, dims, target_ratio, base_q, out_archive, out_len, NULL);
+    return encode_common(vol, vol_on_device, dims, target_ratio, base_q, out_archive, out_len, NULL, VCG_DS_BOX, 0.0f);
+}
+
+static int ds_args_ok(int method, float alpha) {
+    return (method == VCG_DS_BOX || method == VCG_DS_CBOX) && isfinite(alpha);
+}
+
+VC_API vc_status vcg_encode_ds(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
+                               const float base_q[VC_NLOD], int method, float alpha, uint8_t **out_archive,
+                               size_t *out_len) {
+    if (!ds_args_ok(method, alpha)) return VC_ERR_RANGE;
+    return encode_common(vol, vol_on_device, dims, target_ratio, base_q, out_archive, out_len, NULL, method, alpha);
+}
+
+// ---------------------------------------------------------------------------
+// Exporter 2x downscale (tools/downscale.h:48-93) on the device.
+// ---------------------------------------------------------------------------
+static vc_status downscale_common(const uint8_t *in, int on_device, vc_dims d, int method, float alpha, int levels,
+                                  uint8_t *const *out) {
+    if (!in || !out || levels < 1 || levels > 8 || !ds_args_ok(method, alpha)) return VC_ERR_RANGE;
+    if (!d.nx || !d.ny || !d.nz || (uint64_t)d.nx * d.ny > (1ull << 40) / d.nz) return VC_ERR_RANGE;
+    for (int l = 0; l < levels; ++l)
+        if (!out[l]) return VC_ERR_RANGE;
+    if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); return VC_ERR_IO; }
+    const uint32_t dims[3] = {d.nx, d.ny, d.nz};
+    const int rc = vcd_downscale(in, on_device, dims, method, alpha, levels, out);
+    if (rc) report("downscale failed: %s", vcd_last_error());
+    return (vc_status)rc;
+}
+
+VC_API vc_status vcg_downscale2x(const uint8_t *in, int on_device, vc_dims dims, int method, float alpha, uint8_t *out,
+                                 vc_dims *out_dims) {
+    if (out_dims) {
+        out_dims->nx = (dims.nx + 1) / 2;
+        out_dims->ny = (dims.ny + 1) / 2;
+        out_dims->nz = (dims.nz + 1) / 2;
+    }
+    return downscale_common(in, on_device, dims, method, alpha, 1, &out);
+}
+
+VC_API vc_status vcg_downscale_pyramid(const uint8_t *vol_dev, vc_dims dims, int method, float alpha, int levels,
+                                       uint8_t *const *out_dev) {
+    return downscale_common(vol_dev, 1, dims, method, alpha, levels, out_dev);
 }
 
 // ---------------------------------------------------------------------------

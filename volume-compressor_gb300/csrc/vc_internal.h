@@ -125,9 +125,17 @@ typedef struct {
     float q0;           // chosen LOD0 base_q (output)
     uint64_t present0;  // present LOD0 atoms (output)
     uint64_t bytes0;    // LOD0 payload bytes at q0 (output)
+    int ds_method;      // pyramid: 0 the codec's rule (= DS_BOX), 1 DS_CBOX
+    float ds_alpha;     // DS_CBOX push
 } vcd_encode_info;
 int  vcd_encode(const uint8_t *vol, int vol_on_device, vcd_encode_info *info, uint8_t **out,
                 size_t *out_len);
+
+// Exporter 2x downscale (tools/downscale.h): levels 1..levels of the cascade
+// from in; level l into out[l-1]. Device pointers when on_device, else host
+// pointers (staged through device memory).
+int  vcd_downscale(const uint8_t *in, int on_device, const uint32_t dims[3], int method, float alpha, int levels,
+                   uint8_t *const *out);
 
 // Repack into the v2 container (device): one record per non-absent atom slot of
 // the output. flags 1 = present (slot [pay_dst][len][1][dc = first payload

@@ -23,7 +23,8 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook", "vc_open_streaming"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
                "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps",
-               "vcg_set_stream_threads", "vcg_memory_read", "vcg_dct_forward", "vcg_dct_inverse",
+               "vcg_set_stream_threads", "vcg_memory_read", "vcg_downscale2x", "vcg_downscale_pyramid",
+               "vcg_encode_ds", "vcg_dct_forward", "vcg_dct_inverse",
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
@@ -138,6 +139,10 @@ def lib():
         L.vc_open_streaming.restype = P
         L.vc_open_streaming.argtypes = [P, P, ctypes.c_uint64]
         L.vcg_set_stream_threads.argtypes = [ctypes.c_int]
+        L.vcg_downscale2x.argtypes = [P, ctypes.c_int, Dims, ctypes.c_int, ctypes.c_float, P, ctypes.POINTER(Dims)]
+        L.vcg_downscale_pyramid.argtypes = [P, Dims, ctypes.c_int, ctypes.c_float, ctypes.c_int, P]
+        L.vcg_encode_ds.argtypes = [P, ctypes.c_int, Dims, ctypes.c_float, P, ctypes.c_int, ctypes.c_float,
+                                    ctypes.POINTER(P), ctypes.POINTER(ctypes.c_size_t)]
         L.vc_close.argtypes = [P]
         L.vc_lod_dims.argtypes = [P, ctypes.c_int, ctypes.POINTER(Dims)]
         L.vc_decode_lod.argtypes = [P, ctypes.c_int, P, ctypes.POINTER(Dims)]
@@ -295,6 +300,60 @@ def encode_device(dbuf, dims, target_ratio):
     data = ctypes.string_at(out, n.value)
     _libc.free(out)
     return s, data, q0.value
+
+
+DS_BOX, DS_CBOX = 0, 1
+
+
+def ds_dims(dims):
+    return tuple((n + 1) // 2 for n in dims)
+
+
+def downscale2x(vol, method, alpha=0.5):
+    """vcg_downscale2x on a host volume (nz, ny, nx): (status, level-1 array)."""
+    vol = np.ascontiguousarray(vol, np.uint8)
+    nz, ny, nx = vol.shape
+    ox, oy, oz = ds_dims((nx, ny, nz))
+    out = np.zeros((oz, oy, ox), np.uint8)
+    od = Dims()
+    s = lib().vcg_downscale2x(ptr(vol), 0, Dims(nx, ny, nz), method, ctypes.c_float(alpha), ptr(out), ctypes.byref(od))
+    return s, out
+
+
+def downscale_pyramid(dbuf, dims, method, alpha, levels):
+    """vcg_downscale_pyramid of a device volume: (status, [DeviceBuffer per level], [dims per level])."""
+    bufs, dl, d = [], [], tuple(dims)
+    for _ in range(levels):
+        d = ds_dims(d)
+        dl.append(d)
+        bufs.append(DeviceBuffer(max(1, d[0] * d[1] * d[2])))
+    arr = (P * levels)(*[b.ptr for b in bufs])
+    s = lib().vcg_downscale_pyramid(dbuf.ptr, Dims(*dims), method, ctypes.c_float(alpha), levels, arr)
+    return s, bufs, dl
+
+
+def encode_ds(vol, target_ratio, method, alpha=0.5, qs=None, on_device=None):
+    """vcg_encode_ds: the exporter's pyramid; qs None = rate control."""
+    qa = None
+    if qs is not None:
+        qa = np.zeros(8, np.float32)
+        qa[:len(qs)] = qs
+    out, n = P(), ctypes.c_size_t()
+    if on_device is None:
+        vol = np.ascontiguousarray(vol, np.uint8)
+        nz, ny, nx = vol.shape
+        src, flag = ptr(vol), 0
+    else:
+        nx, ny, nz = on_device
+        src, flag = vol.ptr, 1
+    s = lib().vcg_encode_ds(src, flag, Dims(nx, ny, nz), ctypes.c_float(target_ratio),
+                            ptr(qa) if qa is not None else None, method, ctypes.c_float(alpha),
+                            ctypes.byref(out), ctypes.byref(n))
+    if s:
+        return s, None
+    data = ctypes.string_at(out, n.value)
+    _libc.free(out)
+    return s, data
 
 
 def encode_q(vol, target_ratio, qs, on_device=None):
