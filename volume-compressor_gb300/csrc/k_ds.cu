@@ -23,25 +23,29 @@
 
 namespace vcg {
 
+// The DS_CBOX value of one cell from its sum and its chosen voxel.
+__device__ __forceinline__ uint32_t cbox_value(uint32_t sum, uint32_t best, float alpha, bool fused) {
+    const float mean = __fmul_rn(__uint2float_rn(sum), 0.125f);
+    const float d = __fsub_rn(__uint2float_rn(best), mean);
+    const float v = fused ? __fmaf_rn(alpha, d, mean) : __fadd_rn(mean, __fmul_rn(alpha, d));
+    if (v < 0.0f) return 0;
+    if (v > 255.0f) return 255;
+    return (uint32_t)__float2int_rz(__fadd_rn(v, 0.5f));   // 0 for an all-zero cell
+}
+
 template <int M>
 __device__ __forceinline__ uint32_t ds_cell(const uint32_t (&c)[8], float alpha, bool fused) {
     uint32_t sum = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) sum += c[i];
     if (M == 0) return (sum + 4u) >> 3;   // 0 for an all-zero cell, as the reference's short-circuit
-    if (sum == 0) return 0;
-    int best = (int)c[0], bd = -1;
+    // largest 8 |c - mean| (exact), the first in order on ties: one max over
+    // keys deviation << 11 | (7 - i) << 8 | c
+    uint32_t key = 0;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const int d = abs(8 * (int)c[i] - (int)sum);   // 8 |c - mean|, exact
-        if (d > bd) { bd = d; best = (int)c[i]; }
-    }
-    const float mean = __fmul_rn(__uint2float_rn(sum), 0.125f);
-    const float d = __fsub_rn(__int2float_rn(best), mean);
-    const float v = fused ? __fmaf_rn(alpha, d, mean) : __fadd_rn(mean, __fmul_rn(alpha, d));
-    if (v < 0.0f) return 0;
-    if (v > 255.0f) return 255;
-    return (uint32_t)__float2int_rz(__fadd_rn(v, 0.5f));
+    for (int i = 0; i < 8; ++i)
+        key = max(key, (uint32_t)abs(8 * (int)c[i] - (int)sum) << 11 | (uint32_t)(7 - i) << 8 | c[i]);
+    return cbox_value(sum, key & 0xFFu, alpha, fused);
 }
 
 // nx a multiple of 32, in and out 16-byte aligned: one thread makes 16 output
@@ -68,37 +72,32 @@ __global__ void __launch_bounds__(256) k_ds2x_vec(const uint8_t *__restrict__ in
             w[j][0] = a.x; w[j][1] = a.y; w[j][2] = a.z; w[j][3] = a.w;
             w[j][4] = b.x; w[j][5] = b.y; w[j][6] = b.z; w[j][7] = b.w;
         }
-        uint32_t o[4];
-        if (M == 0) {
-            uint32_t r[8];   // r[q]: outputs 2q (bits 0-7) and 2q+1 (bits 16-23)
+        uint32_t r[8];   // r[q]: outputs 2q (bits 0-7) and 2q+1 (bits 16-23)
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < 8; ++q) {
+            if (M == 0) {
                 uint32_t p = 0;
 #pragma unroll
                 for (int j = 0; j < 4; ++j) p += (w[j][q] & 0x00FF00FFu) + ((w[j][q] >> 8) & 0x00FF00FFu);
                 r[q] = ((p + 0x00040004u) >> 3) & 0x00FF00FFu;   // lanes <= 2044: no carry between them
-            }
+            } else {
+                uint32_t res = 0;
 #pragma unroll
-            for (int m = 0; m < 4; ++m) o[m] = __byte_perm(r[2 * m], r[2 * m + 1], 0x6420);
-        } else {
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                uint32_t word = 0;
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {   // output 4m + t: input bytes 8m + 2t, +1 of each row
-                    const int byte = 8 * m + 2 * t;
+                for (int h = 0; h < 2; ++h) {   // output 2q + h: bytes 2h, 2h + 1 of word q of each row
                     uint32_t c[8];
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        const uint32_t wv = w[j][byte >> 2];
-                        c[2 * j] = (wv >> (8 * (byte & 3))) & 0xFFu;
-                        c[2 * j + 1] = (wv >> (8 * ((byte & 3) + 1))) & 0xFFu;
+                        c[2 * j] = (w[j][q] >> (16 * h)) & 0xFFu;
+                        c[2 * j + 1] = (w[j][q] >> (16 * h + 8)) & 0xFFu;
                     }
-                    word |= ds_cell<1>(c, alpha, 16 * k + 4 * m + t >= vec_end) << (8 * t);
+                    res |= ds_cell<1>(c, alpha, 16 * k + 2 * q + h >= vec_end) << (16 * h);
                 }
-                o[m] = word;
+                r[q] = res;
             }
         }
+        uint32_t o[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) o[m] = __byte_perm(r[2 * m], r[2 * m + 1], 0x6420);
         *reinterpret_cast<uint4 *>(out + ((uint64_t)z * oy + y) * ox + 16ull * k) = make_uint4(o[0], o[1], o[2], o[3]);
     }
 }
