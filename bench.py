@@ -47,6 +47,7 @@ def args_parse():
     p.add_argument("--no-served", action="store_true", help="skip the config-5 served-decode measurement")
     p.add_argument("--no-dct", action="store_true", help="skip the config-3 DCT-forms measurement")
     p.add_argument("--no-ds", action="store_true", help="skip the exporter-downscale measurement")
+    p.add_argument("--no-writer", action="store_true", help="skip the writer-append measurement")
     p.add_argument("--no-sweep", action="store_true", help="skip the config-2 target / LOD sweep")
     p.add_argument("--dct-size", type=int, default=1024, help="edge of the DCT-forms volume")
     p.add_argument("--dct-reps", type=int, default=3, help="timed calls per DCT form and direction (0: one call)")
@@ -536,6 +537,93 @@ def downscale_bench(dvol, dims, peak, reps=5, slab=64):
     return res
 
 
+def writer_bench(dvol, dims, q0, g, threads=16, cpu_sample=1024):
+    """The writer API on the 1024^3 volume at the headline's LOD0 base_q: the
+    whole LOD0 through one vc_append_box; through `threads` host threads
+    calling vc_append_atom for every atom (each call waits for its batch: the
+    concurrent calls are encoded together); and through vcg_append_atom_async
+    from one and from `threads` threads, then vcg_writer_flush.
+    Wall clock from vc_create to vc_writer_close (file in a temporary
+    directory); the files must decode to the reference's LOD0. CPU leg: the
+    oracle's atom encoder (transform, quantiser, coder) on `cpu_sample` atoms of
+    the volume with the same number of host threads."""
+    import hashlib
+    import tempfile
+    import threading
+    import numpy as np
+    import vc_gb300 as vc
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oraclelib
+    nx, ny, nz = dims
+    host = dvol.download(nx * ny * nz).reshape(nz, ny, nx)
+    want = g["lod_sha256"][0] if g else None
+    res = {"q0": q0}
+
+    def check(path):
+        a = vc.Archive(open(path, "rb").read())
+        s, out = a.decode_lod(0)
+        a.close()
+        return (s == 0 and hashlib.sha256(out.tobytes()).hexdigest() == want) if want else None
+
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "box.vca")
+        ts = []
+        for _ in range(2):   # the first run sizes the device and pinned buffers
+            t0 = time.perf_counter()
+            w = vc.Writer(path, dims, 10.0)
+            assert w.set_base_q(0, q0) == 0
+            assert w.append_box(0, (0, 0, 0, nx, ny, nz), host) == 0
+            w.close()
+            ts.append(time.perf_counter() - t0)
+        res["append_box"] = {"s": ts[-1], "GBps": nx * ny * nz / ts[-1] / 1e9, "file_bytes": os.path.getsize(path),
+                             "lod0_matches_reference": check(path)}
+        atoms = [(az, ay, ax) for az in range(nz // 32) for ay in range(ny // 32) for ax in range(nx // 32)]
+        blocks = {}
+
+        def block(az, ay, ax):
+            return np.ascontiguousarray(host[az * 32:az * 32 + 32, ay * 32:ay * 32 + 32, ax * 32:ax * 32 + 32])
+
+        for mode, nthreads in (("append_atom", threads), ("append_atom_async", 1), ("append_atom_async", threads)):
+            path = os.path.join(td, f"{mode}_{nthreads}.vca")
+            w = vc.Writer(path, dims, 10.0)
+            assert w.set_base_q(0, q0) == 0
+            bad = []
+            fn = w.append_atom if mode == "append_atom" else w.append_atom_async
+
+            def worker(k):
+                for az, ay, ax in atoms[k::nthreads]:
+                    if fn(0, az, ay, ax, block(az, ay, ax)) != 0:
+                        bad.append((az, ay, ax))
+            th = [threading.Thread(target=worker, args=(k,)) for k in range(nthreads)]
+            t0 = time.perf_counter()
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+            if mode != "append_atom":
+                fs, nf = w.flush()
+                if fs:
+                    bad.append(("flush", fs, nf))
+            w.close()
+            t1 = time.perf_counter() - t0
+            res[f"{mode}_{nthreads}threads"] = {"s": t1, "GBps": nx * ny * nz / t1 / 1e9, "failed": len(bad),
+                                                 "file_bytes": os.path.getsize(path),
+                                                 "lod0_matches_reference": check(path)}
+        del blocks
+    # CPU leg: the oracle's per-atom encode on a sample of atoms
+    O = oraclelib.lib()
+    rng = np.random.default_rng(0xC0DE)
+    ids = np.sort(rng.choice((nx // 32) * (ny // 32) * (nz // 32), cpu_sample, replace=False)).astype(np.uint32)
+    lens = np.zeros(cpu_sample, np.uint32)
+    t0 = time.perf_counter()
+    O.orc_encode_sizes_mt(host.ctypes.data, oraclelib.Dims(nx, ny, nz), ctypes.c_float(q0), ids.ctypes.data,
+                          cpu_sample, lens.ctypes.data, threads)
+    t_cpu = time.perf_counter() - t0
+    res["cpu_port"] = {"GBps": cpu_sample * 32768 / t_cpu / 1e9, "threads": threads, "kind": "port",
+                       "sample": f"{cpu_sample} atoms of the volume, sizes only (no file)"}
+    return res
+
+
 def config3_dct(n=1024, reps=3, sample_atoms=256):
     """Whole-atom integer DCT of the 1024^3 volume, x = vox - dc per atom as the
     codec centres, forward and inverse, in both forms: butterfly (CUDA cores)
@@ -931,6 +1019,9 @@ def gb300_arm(args, dist):
         sweep = config2_sweep(dvol, dims, peak)
     if dist.rank == 0 and not args.no_ds:
         ds = downscale_bench(dvol, dims, peak)
+    writer = None
+    if dist.rank == 0 and not args.no_writer:
+        writer = writer_bench(dvol, dims, q0, g)
     # the other workloads (rank 0): release the headline buffers first
     batched = dct = served = None
     if dist.rank == 0 and not (args.no_batched and args.no_dct and args.no_served):
@@ -982,6 +1073,8 @@ def gb300_arm(args, dist):
         line["config2_sweep"] = sweep
     if ds:
         line["exporter_downscale"] = ds
+    if writer:
+        line["writer_append"] = writer
     print(json.dumps(line), flush=True)
 
 

@@ -62,6 +62,53 @@ typedef struct vc_archive vc_archive;
 vc_status vc_encode(const uint8_t *vol, vc_dims dims, float target_ratio,
                     uint8_t **out_archive, size_t *out_len);
 
+// ---------------------------------------------------------------------------
+// Writer (src/vc/vc.h:42-95, src/vc/vc.c:995-1245): builds a v1 archive file by
+// appending atoms. Atoms are encoded on the GPU; a call returns when its atoms
+// are in the image, as in the reference, and concurrent calls from several
+// threads are encoded together in one device batch. The file layout follows
+// the order in which calls are laid out: a single thread gets exactly the
+// reference's bytes. Thread-safe: many readers and writers may share one handle.
+// ---------------------------------------------------------------------------
+typedef struct vc_writer vc_writer;
+
+// src/vc/vc.h:56 — create (or truncate) the archive file at path for a volume
+// whose LOD0 is lod0_dims. NULL on invalid dims, target_ratio < 1 or an I/O error.
+vc_writer *vc_create(const char *path, vc_dims lod0_dims, float target_ratio);
+
+// src/vc/vc.h:63 — base_q of a LOD, clamped to [0.05, 4096]; an append reads it
+// when it is called. VC_ERR_RANGE for a LOD outside the archive.
+vc_status vc_set_base_q(vc_writer *w, int lod, float q);
+
+// src/vc/vc.h:66 — append one atom. VC_ERR_RANGE for a LOD or atom outside the
+// archive, or a nonzero atom of a LOD without base_q; an all-zero atom is
+// stored KNOWN_ZERO. Appending an atom again replaces it.
+vc_status vc_append_atom(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax,
+                         const uint8_t vox[VC_ATOM3]);
+
+// src/vc/vc.h:73 — append a box of whole atoms (origin and size multiples of
+// 32), raster (z, y, x) order, x fastest; atoms go in (z, y, x) order and the
+// call stops at the first that fails.
+vc_status vc_append_box(vc_writer *w, int lod, vc_box voxel_box, const uint8_t *voxels);
+
+// src/vc/vc.h:78-79 — mark an atom / an index region (atom coords / 32)
+// KNOWN_ZERO without a payload. A region that has a block keeps it.
+vc_status vc_mark_zero_atom(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax);
+vc_status vc_mark_zero_region(vc_writer *w, int lod, uint32_t rz, uint32_t ry, uint32_t rx);
+
+// src/vc/vc.h:84-92 — read back from the writer (decoded on the GPU with the
+// current base_q): an atom as vc_decode_atom would, its coverage, or the 8 atoms
+// of a 2x2x2 block in (dz, dy, dx) order (absent, zero, invalid or outside the
+// LOD: zeros; *any set if one was present).
+vc_status vc_writer_decode_atom(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax,
+                                uint8_t out[VC_ATOM3]);
+vc_cover  vc_writer_coverage(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax);
+vc_status vc_writer_decode_2x2x2(vc_writer *w, int lod, uint32_t az0, uint32_t ay0, uint32_t ax0,
+                                 uint8_t out8[8][VC_ATOM3], int *any);
+
+// src/vc/vc.h:95 — trim the file to its used length and close it (no unlink).
+void vc_writer_close(vc_writer *w);
+
 // src/vc/vc.h:106 — open an archive held in memory. Borrows the buffer: it must
 // outlive the handle. Returns NULL if the header is not a valid v1/v2 header.
 // The archive bytes are copied into device memory on first decode.

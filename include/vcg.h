@@ -118,6 +118,19 @@ vc_status vcg_encode_device(const uint8_t *vol_dev, vc_dims dims, float target_r
 vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
                        const float base_q[VC_NLOD], uint8_t **out_archive, size_t *out_len);
 
+// Asynchronous appends (no counterpart in the reference). vc_append_atom
+// returns once its atom is in the image, which on the GPU costs one pass of the
+// serial range coder per call; a caller that appends many atoms queues them
+// with vcg_append_atom_async (the atom is copied; argument errors return at
+// once) and they are encoded in batches of thousands. Every 8192 queued atoms
+// the appending caller commits them; vcg_writer_flush commits the rest and
+// returns VC_OK or the first failure among the appends queued since the last
+// flush (*failed: how many). Order with the other calls is kept; the readers
+// see a queued atom after the flush; vc_writer_close flushes.
+vc_status vcg_append_atom_async(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax,
+                                const uint8_t vox[VC_ATOM3]);
+vc_status vcg_writer_flush(vc_writer *w, uint64_t *failed);
+
 // The exporter's 2x downscale (tools/downscale.h:29-93) on the GPU. Every
 // output voxel is a function of its own 2x2x2 cell; odd boundaries replicate
 // the edge voxel; output dims are (n + 1) / 2 per axis.

@@ -16,7 +16,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CC = os.environ.get("CC", "gcc")
 
 CU_SRCS = ["vc_device.cu", "vc_encode.cu", "k_decode.cu", "k_encode.cu", "k_synth.cu", "vc_noalloc.cu", "k_batch.cu", "vc_batch.cu", "k_dct.cu", "k_repack.cu", "k_ds.cu"]
-C_SRCS = ["vc_host.c", "vc_server.c"]
+C_SRCS = ["vc_host.c", "vc_server.c", "vc_writer.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xptxas", "-O3",
                      "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off,-O2",

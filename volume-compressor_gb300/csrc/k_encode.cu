@@ -121,9 +121,11 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
         uint32_t az, ay, ax;
         const uint64_t ca = J.first + t;   // canonical index
         J.lay.coords(ca, lod, az, ay, ax);
-        if (lod != cur_lod) {   // uniform across the CTA: quantiser constants of this LOD
-            for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q[lod].dz[i]; qrr[i] = J.q[lod].rr[i]; }
-            cur_lod = lod;
+        const int qi = J.qsel ? (int)J.qsel[t] : lod;
+        if (qi != cur_lod) {   // uniform across the CTA: quantiser constants of this atom
+            __syncthreads();   // every thread is done with the previous constants
+            for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q[qi].dz[i]; qrr[i] = J.q[qi].rr[i]; }
+            cur_lod = qi;
             __syncthreads();
         }
         const bool cached = J.coef && ca < J.coef_n;
@@ -267,12 +269,39 @@ __global__ void __launch_bounds__(128) k_rc_encode(RcJob J) {
     }
     uint8_t *dst = nullptr;
     if (active) {
-        const uint64_t a = J.canon_first + t;   // canonical index
-        const uint64_t off = J.pos[a] + (J.lay.first_in_region(a) ? kL2Bytes : 0ull);
-        dst = J.arc + off;
+        if (J.slot_bytes) {
+            dst = J.arc + t * J.slot_bytes;
+        } else if (J.dst_off) {
+            dst = J.arc + J.dst_off[t];
+        } else {
+            const uint64_t a = J.canon_first + t;   // canonical index
+            dst = J.arc + J.pos[a] + (J.lay.first_in_region(a) ? kL2Bytes : 0ull);
+        }
         dst[0] = (uint8_t)((meta >> 16) & 0xFFu);
     }
-    rc_encode_levels_warp<true>(ent, nnz, active, bstart, active ? dst + 1 : nullptr);
+    const uint32_t nb = rc_encode_levels_warp<true>(ent, nnz, active, bstart, active ? dst + 1 : nullptr,
+                                                    J.slot_bytes ? (uint32_t)(J.slot_bytes - 1) : 0xFFFFFFFFu);
+    if (J.len && t < J.n_atoms) J.len[t] = active ? nb + 1 : 0u;
+}
+
+// one warp per atom: bytes of its slot to its packed offset
+__global__ void k_pack(const uint8_t *slots, uint64_t slot, const uint32_t *len, const uint64_t *off, uint64_t n,
+                       uint8_t *dst) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
+    for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < n; t += nw) {
+        const uint8_t *s = slots + t * slot;
+        uint8_t *d = dst + off[t];
+        const uint32_t l = len[t];
+        for (uint32_t k = lane; k < l; k += 32) d[k] = s[k];
+    }
+}
+
+void launch_pack(const uint8_t *slots, uint64_t slot, const uint32_t *len, const uint64_t *off, uint64_t n,
+                 uint8_t *dst, cudaStream_t s) {
+    if (!n) return;
+    const uint64_t blocks = (n + 7) / 8 < 4096 ? (n + 7) / 8 : 4096;
+    k_pack<<<(unsigned)blocks, 256, 0, s>>>(slots, slot, len, off, n, dst);
 }
 
 // consume[a] = (first atom of its region ? L2 block : 0) + payload length

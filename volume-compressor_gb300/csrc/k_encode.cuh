@@ -45,6 +45,7 @@ struct FwdJob {
     uint64_t first;              // canonical index of this launch's first atom
     uint64_t n_atoms;
     const vcd_quant *q;          // per-LOD quantiser constants (device, [lod])
+    const uint8_t *qsel;         // optional: per atom (this launch) index into q instead of its LOD
     const uint16_t *scan;        // scan position -> raster index
     const uint32_t *alt_mask;
     uint32_t *ent;               // per atom VCD_MAX_ENTRIES slots: scan position | level << 16
@@ -69,6 +70,9 @@ struct RcJob {
     unsigned long long *total_present;
     // write pass
     uint8_t *arc;
+    const uint64_t *dst_off;             // optional: per atom (this launch) payload offset in arc
+    uint64_t slot_bytes;                 // optional: atom t's payload at arc + t * slot_bytes, at most that long
+                                         // (len[t] receives the full length, stored or not)
     const uint64_t *pos;                 // canonical exclusive scan of consumed bytes
     uint64_t canon_first;                // canonical index of this chunk's first atom
     Layout lay;
@@ -90,5 +94,8 @@ void launch_rc_encode(const RcJob &J, bool write, cudaStream_t s);
 void launch_consume(const PlaceJob &J, cudaStream_t s);
 void launch_slots(const PlaceJob &J, cudaStream_t s);
 void launch_gather_dc(const uint32_t *meta, uint64_t n, uint8_t *dc, cudaStream_t s);
+// payloads of n atoms from fixed slots (slot bytes apart) to packed offsets
+void launch_pack(const uint8_t *slots, uint64_t slot, const uint32_t *len, const uint64_t *off, uint64_t n,
+                 uint8_t *dst, cudaStream_t s);
 
 }  // namespace vcg

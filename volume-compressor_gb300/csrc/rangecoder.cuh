@@ -288,9 +288,10 @@ struct RcEnc {
     uint32_t range, pending, nbytes;
     uint32_t cache;
     uint8_t *out;
+    uint32_t cap;   // bytes stored at most (the count goes on past it)
 
-    __device__ __forceinline__ void init(uint8_t *o) {
-        low = 0; range = 0xFFFFFFFFu; pending = 1; nbytes = 0; cache = 0; out = o;
+    __device__ __forceinline__ void init(uint8_t *o, uint32_t c) {
+        low = 0; range = 0xFFFFFFFFu; pending = 1; nbytes = 0; cache = 0; out = o; cap = c;
     }
     __device__ __forceinline__ void shift_low() {   // src/vc/vc.c:369-380
         if (!WRITE) { ++nbytes; return; }
@@ -298,7 +299,8 @@ struct RcEnc {
             uint32_t carry = (uint32_t)(low >> 32);
             uint32_t c = cache;
             do {
-                out[nbytes++] = (uint8_t)(c + carry);
+                if (nbytes < cap) out[nbytes] = (uint8_t)(c + carry);
+                ++nbytes;
                 c = 0xFFu;
             } while (--pending);
             cache = (uint32_t)(low >> 24) & 0xFFu;
@@ -347,12 +349,13 @@ __device__ __forceinline__ void enc_byp(bool on, bool bit, RcEnc<WRITE> &e) {
 // Every lane of the warp must call this together; `active` lanes encode their
 // list ent[0..nnz) (scan position | level << 16, 16-byte aligned) and return
 // the coder byte count (inactive lanes return 0): the reference encoder's bytes
-// (src/vc/vc.c:471-490, 512-544).
+// (src/vc/vc.c:471-490, 512-544). At most `cap` bytes are stored.
 template <bool WRITE>
 __device__ __forceinline__ uint32_t rc_encode_levels_warp(const uint32_t *ent, uint32_t nnz, bool active,
-                                                          const uint32_t *band_start, uint8_t *out) {
+                                                          const uint32_t *band_start, uint8_t *out,
+                                                          uint32_t cap = 0xFFFFFFFFu) {
     RcEnc<WRITE> e;
-    e.init(out);
+    e.init(out, cap);
     if (!active) nnz = 0;
     auto load4 = [&](uint32_t j) -> uint4 {
         return j < nnz ? __ldg(reinterpret_cast<const uint4 *>(ent + j)) : make_uint4(0, 0, 0, 0);

@@ -70,6 +70,7 @@ static void ctx_free(void *p) {
         if (c->buf[i]) cudaFree(c->buf[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->stage_host) cudaFreeHost(c->stage_host);
+    if (c->wpin) cudaFreeHost(c->wpin);
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     if (c->copy_stream) {
         for (int i = 0; i < 16; ++i) cudaEventDestroy(c->chunk_ev[i]);
@@ -107,7 +108,10 @@ int vcd_prof_on(void) { return g_prof; }
 
 float vcd_elapsed(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        cudaGetLastError();   // a timing that cannot be read is not an error of the next call
+        ms = 0.f;
+    }
     return ms;
 }
 
@@ -267,8 +271,11 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     J.nnz_total = (unsigned long long *)((uint8_t *)p_ctl + 8);
     memcpy(J.band_start, g_dev.band_start, sizeof J.band_start);
 
-    cudaMemsetAsync(p_ctl, 0, 16, c->stream);
-    cudaMemsetAsync(p_err, 0xFF, 4, c->stream);
+    if ((e = cudaMemsetAsync(p_ctl, 0, 16, c->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(p_err, 0xFF, 4, c->stream)) != cudaSuccess) {
+        vcd_set_error("decode control words", e);
+        return vcd_status_of(e);
+    }
     StageEvents ev;
     memcpy(ev.ev, c->ev, sizeof ev.ev);
     uint64_t ctl_h[2] = {0xFFFFFFFFull, 0};
@@ -321,8 +328,23 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
             cudaEventRecord(ev.ev[3], c->stream);
         }
     } else {
-        launch_decode(J, g_dev.num_sms, c->stream, &ev);
-        cudaMemcpyAsync(ctl_h, p_ctl, 16, cudaMemcpyDeviceToHost, c->stream);
+        launch_decode_front(J, g_dev.num_sms, c->stream, &ev);
+        if ((e = cudaPeekAtLastError()) != cudaSuccess) {
+            vcd_set_error("decode launch (lists, range decoder)", e);
+            cudaGetLastError();
+            return vcd_status_of(e);
+        }
+        launch_idct(J, g_dev.num_sms, c->stream, 0, n);
+        cudaEventRecord(ev.ev[3], c->stream);
+        if ((e = cudaPeekAtLastError()) != cudaSuccess) {
+            vcd_set_error("decode launch (inverse transform)", e);
+            cudaGetLastError();
+            return vcd_status_of(e);
+        }
+        if ((e = cudaMemcpyAsync(ctl_h, p_ctl, 16, cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) {
+            vcd_set_error("decode status copy", e);
+            return vcd_status_of(e);
+        }
     }
     if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess || (piped && (e = cudaStreamSynchronize(c->copy_stream)) != cudaSuccess) ||
         (e = cudaGetLastError()) != cudaSuccess) {
@@ -453,7 +475,11 @@ extern "C" int vcd_decode_staged(vcd_archive *d, const vcd_region *r, size_t tab
         return 4;
     uint8_t *stg = (uint8_t *)c->buf[VCD_BUF_STG];
     // 16 zero bytes after the last payload, as after a resident archive
-    cudaMemsetAsync(stg + arena_off + arena_bytes, 0, 16, c->stream);
+    cudaError_t e = cudaMemsetAsync(stg + arena_off + arena_bytes, 0, 16, c->stream);
+    if (e != cudaSuccess) {
+        vcd_set_error("staging slack", e);
+        return vcd_status_of(e);
+    }
     const int rc = decode_job(c, stg + arena_off, (const vcd_atom *)(stg + table_off), 1, d->dq + r->lod, r, out_dev,
                               out_host, out_bytes, c->stage_started ? c->ev[4] : NULL);
     c->stage_started = 0;

@@ -11,7 +11,7 @@ enum {
     VCD_BUF_VOL, VCD_BUF_PYR, VCD_BUF_EENT, VCD_BUF_EMETA, VCD_BUF_LEN, VCD_BUF_POS, VCD_BUF_ARC,
     VCD_BUF_BEST, VCD_BUF_RED,
     VCD_BUF_BUA, VCD_BUF_BDST, VCD_BUF_BREQ, VCD_BUF_BOFF, VCD_BUF_BCNT, VCD_BUF_BENT, VCD_BUF_BCTL, VCD_BUF_BOUT,
-    VCD_BUF_BPIN, VCD_BUF_COEF, VCD_BUF_RPK, VCD_BUF_RPKREC, VCD_BUF_STG,
+    VCD_BUF_BPIN, VCD_BUF_COEF, VCD_BUF_RPK, VCD_BUF_RPKREC, VCD_BUF_STG, VCD_BUF_WPACK,
     VCD_NBUF
 };
 
@@ -34,6 +34,9 @@ struct vcd_ctx {
     uint8_t *stage_host;
     size_t stage_cap;
     int stage_started;           // an upload of the current call was issued (ev[4] recorded)
+    // writer batches: payloads copied back from the device
+    uint8_t *wpin;
+    size_t wpin_cap;
 };
 
 // Kernel statistics, accumulated while profiling is enabled (vcg_profile_enable).

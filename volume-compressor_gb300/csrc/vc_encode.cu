@@ -61,6 +61,7 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
     for (uint64_t c0 = a0; c0 < a1; c0 += kChunk) {
         const uint64_t n = a1 - c0 < kChunk ? a1 - c0 : kChunk;
         FwdJob F;
+        memset(&F, 0, sizeof F);   // fields this pass does not use stay null
         F.lay = S.lay;
         memcpy(F.vol, S.lvol, sizeof F.vol);
         memcpy(F.dims, S.dims, sizeof F.dims);
@@ -246,6 +247,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     // ---- canonical placement: exclusive scan of consumed bytes
     const uint64_t head = 128 + 16 * info->l1_cap;
     PlaceJob P;
+    memset(&P, 0, sizeof P);
     P.n_total = total_atoms;
     P.pos = S.pos;
     P.len = S.len;
@@ -332,5 +334,140 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     }
     *out = res;
     *out_len = total;
+    return 0;
+}
+
+// ---------------------------------------------------------------- writer batches
+// Independent atoms (box rasters or stacked single atoms) through the same
+// forward and coder kernels as the whole-volume encoder, with one coder pass:
+// per chunk of at most kWChunk atoms a forward pass and a writing coder pass
+// into fixed slots of kSlot bytes (the reference encoder's largest atom:
+// 1 + 4 * 32768 + 64 bytes, rounded up), the lengths back to the host for the
+// packing offsets, and a packing kernel whose output is copied into the
+// thread's pinned buffer. An atom longer than its slot (where the reference's
+// encoder stops with "range encoder overflow") makes its chunk take a second,
+// exact writing pass.
+static const uint64_t kWChunk = 8192;
+static const uint64_t kSlot = 131200;
+
+extern "C" int vcd_encode_segments(const vcd_seg *segs, int nseg, const float *qs, int nq, uint8_t **pay,
+                                   uint64_t *pay_bytes) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    if (nq < 1 || nq > 256) return 2;
+    cudaStream_t st = c->stream;
+    void *p;
+    const size_t q_b = ((size_t)nq * sizeof(vcd_quant) + 255) & ~(size_t)255;
+    CK(vcd_scratch(c, VCD_BUF_EMETA, q_b + kWChunk * (4 + 4 + 8 + 1) + 256, &p), "writer metadata");
+    vcd_quant *qtab = (vcd_quant *)p;
+    uint32_t *dmeta = (uint32_t *)((uint8_t *)p + q_b);
+    uint32_t *dlen = dmeta + kWChunk;
+    uint64_t *doff = (uint64_t *)(dlen + kWChunk);
+    uint8_t *dqsel = (uint8_t *)(doff + kWChunk);
+    vcd_quant *qh = (vcd_quant *)malloc((size_t)nq * sizeof(vcd_quant));
+    uint64_t *offh = (uint64_t *)malloc(kWChunk * sizeof(uint64_t));
+    if (!qh || !offh) { free(qh); free(offh); return 3; }
+    for (int i = 0; i < nq; ++i) vch_quant_consts(qs[i], &qh[i]);
+    cudaError_t e = cudaEventRecord(c->ev[6], st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(qtab, qh, (size_t)nq * sizeof(vcd_quant), cudaMemcpyHostToDevice, st);
+    uint64_t total = 0;
+    for (int sg = 0; sg < nseg && e == cudaSuccess; ++sg) {
+        const vcd_seg &S = segs[sg];
+        const uint64_t acx = S.nx / 32, acy = S.ny / 32, acz = S.nz / 32, na = acx * acy * acz;
+        if (!na) continue;
+        if ((e = vcd_scratch(c, VCD_BUF_VOL, (size_t)S.nx * S.ny * S.nz + 16, &p)) != cudaSuccess) break;
+        const uint8_t *dvol = (const uint8_t *)p;
+        if ((e = cudaMemcpyAsync(p, S.vox, (size_t)S.nx * S.ny * S.nz, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            break;
+        Layout lay;
+        memset(&lay, 0, sizeof lay);
+        lay.nlod = 1;
+        for (int l = 1; l <= 8; ++l) lay.base[l] = na;
+        lay.acx[0] = (uint32_t)acx; lay.acy[0] = (uint32_t)acy; lay.acz[0] = (uint32_t)acz;
+        for (uint64_t c0 = 0; c0 < na && e == cudaSuccess; c0 += kWChunk) {
+            const uint64_t n = na - c0 < kWChunk ? na - c0 : kWChunk;
+            if ((e = vcd_scratch(c, VCD_BUF_EENT, n * VCD_MAX_ENTRIES * 4 + 16, &p)) != cudaSuccess) break;
+            uint32_t *ent = (uint32_t *)p;
+            if ((e = cudaMemcpyAsync(dqsel, S.qsel + c0, n, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+            FwdJob F;
+            memset(&F, 0, sizeof F);
+            F.lay = lay;
+            F.vol[0] = dvol;
+            F.dims[0][0] = S.nx; F.dims[0][1] = S.ny; F.dims[0][2] = S.nz;
+            F.first = c0;
+            F.n_atoms = n;
+            F.q = qtab;
+            F.qsel = dqsel;
+            F.scan = g_dev.tables->scan;
+            F.alt_mask = g_dev.tables->alt_mask;
+            F.ent = ent;
+            F.meta = dmeta;
+            launch_fwd(F, g_dev.num_sms, st);
+            if ((e = vcd_scratch(c, VCD_BUF_ARC, n * kSlot + 16, &p)) != cudaSuccess) break;
+            uint8_t *dslots = (uint8_t *)p;
+            RcJob W;
+            memset(&W, 0, sizeof W);
+            W.n_atoms = n;
+            W.meta = dmeta;
+            W.ent = ent;
+            memcpy(W.band_start, g_dev.band_start, sizeof W.band_start);
+            W.arc = dslots;
+            W.slot_bytes = kSlot;
+            W.len = dlen;
+            launch_rc_encode(W, true, st);
+            if ((e = cudaMemcpyAsync(S.len + c0, dlen, n * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(st)) != cudaSuccess)
+                break;
+            uint64_t bytes = 0;
+            bool over = false;
+            for (uint64_t i = 0; i < n; ++i) {
+                offh[i] = bytes;
+                S.off[c0 + i] = total + bytes;
+                bytes += S.len[c0 + i];
+                over |= S.len[c0 + i] > kSlot;
+            }
+            if ((e = vcd_scratch(c, VCD_BUF_WPACK, bytes + 16, &p)) != cudaSuccess) break;
+            uint8_t *dpack = (uint8_t *)p;
+            if ((e = cudaMemcpyAsync(doff, offh, n * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+            if (!over) {
+                launch_pack(dslots, kSlot, dlen, doff, n, dpack, st);
+            } else {   // exact second pass for a chunk with an atom longer than its slot
+                W.slot_bytes = 0;
+                W.len = nullptr;
+                W.arc = dpack;
+                W.dst_off = doff;
+                launch_rc_encode(W, true, st);
+            }
+            if (total + bytes > c->wpin_cap) {   // grow the pinned output, keeping what it holds
+                if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
+                size_t want = (total + bytes) + (total + bytes) / 2 + (1 << 20);
+                uint8_t *np_ = NULL;
+                if ((e = cudaMallocHost(&np_, want)) != cudaSuccess) break;
+                if (c->wpin) {
+                    memcpy(np_, c->wpin, total);
+                    cudaFreeHost(c->wpin);
+                }
+                c->wpin = np_;
+                c->wpin_cap = want;
+            }
+            if (bytes && (e = cudaMemcpyAsync(c->wpin + total, dpack, bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+                break;
+            // offh and the staging are reused by the next chunk
+            if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
+            total += bytes;
+        }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev[7], st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    free(qh);
+    free(offh);
+    if (e != cudaSuccess) {
+        vcd_set_error("writer batch", e);
+        return vcd_status_of(e);
+    }
+    c->last_ms = vcd_elapsed(c->ev[6], c->ev[7]);
+    *pay = c->wpin;
+    *pay_bytes = total;
     return 0;
 }

@@ -160,6 +160,7 @@ struct vc_archive {
     uint64_t lod_base[VC_NLOD + 1];
     vcd_archive *dev;
     vcd_archive *sdev;      // streamed decode: dequantisation tables only
+    int view;               // a writer's live view: no streaming payload limit, bad slots of a 2x2x2 read as empty
 };
 
 // Bytes [off, off + len) of the archive: a pointer into a flat archive's
@@ -505,7 +506,8 @@ static int stream_device(vc_archive *a) {   // dequantisation tables on the devi
     return rc;
 }
 
-static vc_status decode_box_streamed(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev) {
+static vc_status decode_box_streamed(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev,
+                                     int bad_as_empty, uint64_t *n_present) {
     if (stream_device(a) != 0) return VC_ERR_IO;
     const vc_dims d = lod_dims_of(a->d0, lod);
     vcd_region r;
@@ -561,7 +563,9 @@ static vc_status decode_box_streamed(vc_archive *a, int lod, vc_box b, uint8_t *
                         fl = slot_of(a, bk, az, ay, ax + i, &off, &len, &dc);
                     }
                     if (fl != 1) { t->kind = VCD_EMPTY; continue; }
-                    if (off == NO_OFFSET || len < 1 || off > a->len || len > a->len - off || len > STREAM_PAYLOAD_MAX) {
+                    if (off == NO_OFFSET || len < 1 || off > a->len || len > a->len - off ||
+                        (len > STREAM_PAYLOAD_MAX && !a->view)) {
+                        if (bad_as_empty) { t->kind = VCD_EMPTY; continue; }
                         nb = t0 + i;
                         break;
                     }
@@ -643,6 +647,7 @@ static vc_status decode_box_streamed(vc_archive *a, int lod, vc_box b, uint8_t *
     r.cap_total = cap;
     r.payload_bytes = bytes;
     r.present = present;
+    if (n_present) *n_present = present;
     e = vcd_decode_staged(a->sdev, &r, 0, arena_off, pay, out_dev, out, out_bytes);
     if (e && e != VC_ERR_FORMAT) report("streamed decode: %s", vcd_last_error());
     st = (vc_status)e;
@@ -655,7 +660,8 @@ out:
 // Shared by decode_region / decode_atom / decode_lod: out_dev (device) or out
 // (host) receives the box raster.
 static vc_status decode_box(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev) {
-    if (a->read && __atomic_load_n(&a->resident, __ATOMIC_ACQUIRE) != 1) return decode_box_streamed(a, lod, b, out, out_dev);
+    if (a->read && __atomic_load_n(&a->resident, __ATOMIC_ACQUIRE) != 1)
+        return decode_box_streamed(a, lod, b, out, out_dev, 0, NULL);
     if (make_resident(a) != 0) return VC_ERR_IO;
     vc_dims d = lod_dims_of(a->d0, lod);
     vcd_region r;
@@ -975,6 +981,64 @@ VC_API vc_status vcg_downscale2x(const uint8_t *in, int on_device, vc_dims dims,
 VC_API vc_status vcg_downscale_pyramid(const uint8_t *vol_dev, vc_dims dims, int method, float alpha, int levels,
                                        uint8_t *const *out_dev) {
     return downscale_common(vol_dev, 1, dims, method, alpha, levels, out_dev);
+}
+
+// ---------------------------------------------------------------------------
+// Live view of a writer's image (vc_writer.c; src/vc/vc.c:1475-1530): a v1
+// archive read through a callback over the image, whose length and base_q
+// follow the writer. Only the writer changes it, while no reader uses it.
+// ---------------------------------------------------------------------------
+vc_archive *vch_view_new(vc_read_fn read, void *ud, vc_dims d0, int nlod, uint64_t l1_off, uint64_t l1_cap) {
+    vc_archive *a = (vc_archive *)calloc(1, sizeof *a);
+    if (!a) return NULL;
+    a->read = read;
+    a->ud = ud;
+    a->d0 = d0;
+    a->nlod = nlod;
+    a->version = 1;
+    a->l1_off = l1_off;
+    a->l1_cap = l1_cap;
+    a->view = 1;
+    pthread_mutex_init(&a->mu, NULL);
+    return a;
+}
+
+void vch_view_set(vc_archive *a, uint64_t len, const float *base_q) {
+    a->len = len;
+    if (memcmp(a->base_q, base_q, sizeof a->base_q)) {
+        memcpy(a->base_q, base_q, sizeof a->base_q);
+        if (a->sdev) { vcd_free_archive(a->sdev); a->sdev = NULL; }   // dequantisation tables follow base_q
+    }
+}
+
+// src/vc/vc.c:1507-1530: the 8 atoms (dz, dy, dx) from (az0, ay0, ax0); atoms
+// outside the LOD and atoms without a valid payload read as zeros.
+vc_status vch_view_decode_2x2x2(vc_archive *a, int lod, uint32_t az0, uint32_t ay0, uint32_t ax0,
+                                uint8_t out8[8][VC_ATOM3], int *any) {
+    if (!a || lod < 0 || lod >= a->nlod || !out8) return VC_ERR_RANGE;
+    const vc_dims d = lod_dims_of(a->d0, lod);
+    const uint32_t acx = (d.nx + 31) / 32, acy = (d.ny + 31) / 32, acz = (d.nz + 31) / 32;
+    memset(out8, 0, 8 * (size_t)VC_ATOM3);
+    if (any) *any = 0;
+    if (ax0 >= acx || ay0 >= acy || az0 >= acz) return VC_OK;
+    const uint32_t nx = ax0 + 2 <= acx ? 2 : 1, ny = ay0 + 2 <= acy ? 2 : 1, nz = az0 + 2 <= acz ? 2 : 1;
+    const vc_box b = {ax0 * 32, ay0 * 32, az0 * 32, (ax0 + nx) * 32, (ay0 + ny) * 32, (az0 + nz) * 32};
+    uint8_t *box = (uint8_t *)malloc((size_t)nx * ny * nz * VC_ATOM3);
+    if (!box) return VC_ERR_OOM;
+    uint64_t present = 0;
+    const vc_status s = decode_box_streamed(a, lod, b, box, NULL, 1, &present);
+    if (s == VC_OK) {
+        for (uint32_t dz = 0; dz < nz; ++dz)
+            for (uint32_t dy = 0; dy < ny; ++dy)
+                for (uint32_t dx = 0; dx < nx; ++dx)
+                    for (uint32_t z = 0; z < 32; ++z)
+                        for (uint32_t y = 0; y < 32; ++y)
+                            memcpy(&out8[(dz * 2 + dy) * 2 + dx][(z * 32 + y) * 32],
+                                   box + (((size_t)(dz * 32 + z) * ny * 32 + dy * 32 + y) * nx * 32 + dx * 32), 32);
+        if (any) *any = present > 0;
+    }
+    free(box);
+    return s;
 }
 
 // ---------------------------------------------------------------------------

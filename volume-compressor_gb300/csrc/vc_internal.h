@@ -131,6 +131,22 @@ typedef struct {
 int  vcd_encode(const uint8_t *vol, int vol_on_device, vcd_encode_info *info, uint8_t **out,
                 size_t *out_len);
 
+// Writer batches: independent atoms encoded on the device. A segment is a host
+// raster (x fastest) of nx x ny x nz voxels, each a multiple of 32, whose atoms
+// (raster order of its atom grid) are encoded each with the quantiser qs[qsel[i]]
+// (src/vc/vc.c:595-622). len[i] receives the payload bytes ([dc][coder bytes];
+// 0 for an all-zero atom) and off[i] the payload's offset in *pay, where all
+// payloads of all segments are packed in segment order (a pinned buffer owned by
+// the calling thread, valid until its next call).
+typedef struct {
+    const uint8_t *vox;
+    uint32_t nx, ny, nz;
+    const uint8_t *qsel;
+    uint32_t *len;
+    uint64_t *off;
+} vcd_seg;
+int  vcd_encode_segments(const vcd_seg *segs, int nseg, const float *qs, int nq, uint8_t **pay, uint64_t *pay_bytes);
+
 // Exporter 2x downscale (tools/downscale.h): levels 1..levels of the cascade
 // from in; level l into out[l-1]. Device pointers when on_device, else host
 // pointers (staged through device memory).

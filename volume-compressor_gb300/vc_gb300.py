@@ -20,10 +20,14 @@ VC_ABSENT, VC_KNOWN_ZERO, VC_PRESENT = 0, 1, 2
 # Every symbol the public headers declare (checked by the CPU test suite).
 VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod", "vc_decode_atom",
               "vc_decode_region", "vc_atom_coverage", "vc_atom_payload_range", "vc_archive_version",
-              "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook", "vc_open_streaming"]
+              "vc_region_blob_range", "vc_region_atoms", "vc_set_panic_hook", "vc_open_streaming",
+              "vc_create", "vc_set_base_q", "vc_append_atom", "vc_append_box", "vc_mark_zero_atom",
+              "vc_mark_zero_region", "vc_writer_decode_atom", "vc_writer_coverage", "vc_writer_decode_2x2x2",
+              "vc_writer_close"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
                "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps",
                "vcg_set_stream_threads", "vcg_memory_read", "vcg_downscale2x", "vcg_downscale_pyramid",
+               "vcg_append_atom_async", "vcg_writer_flush",
                "vcg_encode_ds", "vcg_dct_forward", "vcg_dct_inverse",
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
@@ -137,6 +141,20 @@ def lib():
         L.vc_open.restype = P
         L.vc_open.argtypes = [P, ctypes.c_size_t]
         L.vc_open_streaming.restype = P
+        u32 = ctypes.c_uint32
+        L.vc_create.restype = P
+        L.vc_create.argtypes = [ctypes.c_char_p, Dims, ctypes.c_float]
+        L.vc_set_base_q.argtypes = [P, ctypes.c_int, ctypes.c_float]
+        L.vc_append_atom.argtypes = [P, ctypes.c_int, u32, u32, u32, P]
+        L.vc_append_box.argtypes = [P, ctypes.c_int, Box, P]
+        L.vc_mark_zero_atom.argtypes = [P, ctypes.c_int, u32, u32, u32]
+        L.vc_mark_zero_region.argtypes = [P, ctypes.c_int, u32, u32, u32]
+        L.vc_writer_decode_atom.argtypes = [P, ctypes.c_int, u32, u32, u32, P]
+        L.vc_writer_coverage.argtypes = [P, ctypes.c_int, u32, u32, u32]
+        L.vc_writer_decode_2x2x2.argtypes = [P, ctypes.c_int, u32, u32, u32, P, ctypes.POINTER(ctypes.c_int)]
+        L.vc_writer_close.argtypes = [P]
+        L.vcg_append_atom_async.argtypes = [P, ctypes.c_int, u32, u32, u32, P]
+        L.vcg_writer_flush.argtypes = [P, ctypes.POINTER(ctypes.c_uint64)]
         L.vc_open_streaming.argtypes = [P, P, ctypes.c_uint64]
         L.vcg_set_stream_threads.argtypes = [ctypes.c_int]
         L.vcg_downscale2x.argtypes = [P, ctypes.c_int, Dims, ctypes.c_int, ctypes.c_float, P, ctypes.POINTER(Dims)]
@@ -512,6 +530,67 @@ class StreamingArchive(Archive):
     def reads(self):
         """(calls, bytes) served by the native memory source."""
         return (self.src.reads, self.src.bytes) if self.src is not None else None
+
+
+class Writer:
+    """vc_create / vc_append_* / vc_mark_zero_* / vc_writer_* / vc_writer_close."""
+
+    def __init__(self, path, dims, target_ratio):
+        self.path = path
+        self.h = lib().vc_create(path.encode(), Dims(*dims), ctypes.c_float(target_ratio))
+
+    def __bool__(self):
+        return bool(self.h)
+
+    def set_base_q(self, lod, q):
+        return lib().vc_set_base_q(self.h, lod, ctypes.c_float(q))
+
+    def append_atom(self, lod, az, ay, ax, vox):
+        vox = np.ascontiguousarray(vox, np.uint8)
+        return lib().vc_append_atom(self.h, lod, az, ay, ax, ptr(vox))
+
+    def append_box(self, lod, box, voxels):
+        voxels = np.ascontiguousarray(voxels, np.uint8)
+        return lib().vc_append_box(self.h, lod, Box(*box), ptr(voxels))
+
+    def append_atom_async(self, lod, az, ay, ax, vox):
+        vox = np.ascontiguousarray(vox, np.uint8)
+        return lib().vcg_append_atom_async(self.h, lod, az, ay, ax, ptr(vox))
+
+    def flush(self):
+        """vcg_writer_flush: (status, failed count)."""
+        n = ctypes.c_uint64()
+        return lib().vcg_writer_flush(self.h, ctypes.byref(n)), n.value
+
+    def mark_zero_atom(self, lod, az, ay, ax):
+        return lib().vc_mark_zero_atom(self.h, lod, az, ay, ax)
+
+    def mark_zero_region(self, lod, rz, ry, rx):
+        return lib().vc_mark_zero_region(self.h, lod, rz, ry, rx)
+
+    def coverage(self, lod, az, ay, ax):
+        return lib().vc_writer_coverage(self.h, lod, az, ay, ax)
+
+    def decode_atom(self, lod, az, ay, ax):
+        out = np.zeros(32768, np.uint8)
+        return lib().vc_writer_decode_atom(self.h, lod, az, ay, ax, ptr(out)), out
+
+    def decode_2x2x2(self, lod, az0, ay0, ax0):
+        out = np.zeros((8, 32768), np.uint8)
+        anyv = ctypes.c_int()
+        s = lib().vc_writer_decode_2x2x2(self.h, lod, az0, ay0, ax0, ptr(out), ctypes.byref(anyv))
+        return s, anyv.value, out
+
+    def close(self):
+        if self.h:
+            lib().vc_writer_close(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def set_stream_threads(n):
