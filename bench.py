@@ -537,11 +537,12 @@ def downscale_bench(dvol, dims, peak, reps=5, slab=64):
     return res
 
 
-def writer_bench(dvol, dims, q0, g, threads=16, cpu_sample=1024):
+def writer_bench(dvol, dims, q0, g, threads=16, cpu_sample=1024, sync_atoms=2048):
     """The writer API on the 1024^3 volume at the headline's LOD0 base_q: the
     whole LOD0 through one vc_append_box; through `threads` host threads
     calling vc_append_atom for every atom (each call waits for its batch: the
-    concurrent calls are encoded together); and through vcg_append_atom_async
+    concurrent calls are encoded together; timed on the first `sync_atoms`
+    atoms); and through vcg_append_atom_async
     from one and from `threads` threads, then vcg_writer_flush.
     Wall clock from vc_create to vc_writer_close (file in a temporary
     directory); the files must decode to the reference's LOD0. CPU leg: the
@@ -589,9 +590,11 @@ def writer_bench(dvol, dims, q0, g, threads=16, cpu_sample=1024):
             assert w.set_base_q(0, q0) == 0
             bad = []
             fn = w.append_atom if mode == "append_atom" else w.append_atom_async
+            # each synchronous call waits for one coder chain: time it on the first sync_atoms atoms
+            todo = atoms[:sync_atoms] if mode == "append_atom" else atoms
 
             def worker(k):
-                for az, ay, ax in atoms[k::nthreads]:
+                for az, ay, ax in todo[k::nthreads]:
                     if fn(0, az, ay, ax, block(az, ay, ax)) != 0:
                         bad.append((az, ay, ax))
             th = [threading.Thread(target=worker, args=(k,)) for k in range(nthreads)]
@@ -606,9 +609,11 @@ def writer_bench(dvol, dims, q0, g, threads=16, cpu_sample=1024):
                     bad.append(("flush", fs, nf))
             w.close()
             t1 = time.perf_counter() - t0
-            res[f"{mode}_{nthreads}threads"] = {"s": t1, "GBps": nx * ny * nz / t1 / 1e9, "failed": len(bad),
-                                                 "file_bytes": os.path.getsize(path),
-                                                 "lod0_matches_reference": check(path)}
+            row = {"atoms": len(todo), "s": t1, "GBps": len(todo) * 32768 / t1 / 1e9, "failed": len(bad),
+                   "file_bytes": os.path.getsize(path)}
+            if len(todo) == len(atoms):
+                row["lod0_matches_reference"] = check(path)
+            res[f"{mode}_{nthreads}threads"] = row
         del blocks
     # CPU leg: the oracle's per-atom encode on a sample of atoms
     O = oraclelib.lib()
