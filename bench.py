@@ -224,6 +224,55 @@ def cpu_decode_setup(size, target, threads):
     return data, q0
 
 
+def host_info():
+    """The host CPU (model name) and its logical core count."""
+    import subprocess
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"cpu_model": model, "nproc": os.cpu_count()}
+
+
+def cpu_one_thread(data, n_atoms=512):
+    """One host thread decoding a sample of LOD0 atoms with the CPU decoder that
+    cpu_decoder uses: (GB/s, kind, sample)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    ref_so = os.path.join(ROOT, "oracle", "_ref", "libvcref.so")
+    if os.path.exists(ref_so):
+        sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+        import refcodec
+        a, kind = refcodec.RefArchive(data), "reference"
+    else:
+        import oraclelib
+        a, kind = oraclelib.Archive(data), "port"
+    _, (nx, ny, nz) = a.lod_dims(0)
+    atoms = [(ax, ay, az) for az in range((nz + 31) // 32) for ay in range((ny + 31) // 32)
+             for ax in range((nx + 31) // 32)]
+    pick = np.random.default_rng(0x1CE).choice(len(atoms), min(n_atoms, len(atoms)), replace=False)
+    t0 = time.perf_counter()
+    for i in pick:
+        ax, ay, az = atoms[int(i)]
+        s, _ = a.decode_atom(0, ax, ay, az)
+        assert s == 0
+    dt = time.perf_counter() - t0
+    return len(pick) * 32768 / dt / 1e9, kind, f"{len(pick)} LOD0 atoms chosen at random, one host thread"
+
+
 def cpu_decoder(data, threads):
     """Returns (kind, decode_fn) timing a full LOD0 decode on the host cores."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -899,8 +948,9 @@ def reference_arm(args, dist):
             "data": "synthetic",
             "config": {"workload": f"LOD0 decode, {args.size}^3 u8 synthetic scroll volume, target_ratio "
                                    f"{args.target:g}", "q0": q0, "archive_bytes": len(data)},
-            "cpu_baseline": {"value": gbps, "unit": "GB/s", "cores": threads, "kind": kind,
-                             "sample": f"full LOD0 decode ({nbytes} voxels) per step, parallel-for over atoms"},
+            "cpu_baseline": dict({"value": gbps, "unit": "GB/s", "cores": threads, "kind": kind,
+                                  "sample": f"full LOD0 decode ({nbytes} voxels) per step, parallel-for over atoms"},
+                                 **host_info()),
             "e2e": {"value": gbps, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -1016,6 +1066,9 @@ def gb300_arm(args, dist):
         dt = time.perf_counter() - t0
         cpu = {"value": nbytes / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": kind,
                "sample": f"one full LOD0 decode ({nbytes} voxels) of the same archive, parallel-for over atoms"}
+        v1, k1, s1 = cpu_one_thread(data)
+        cpu["one_thread"] = {"value": v1, "unit": "GB/s", "kind": k1, "sample": s1}
+        cpu.update(host_info())
         if lod0_ok is None:
             lod0_ok = bool(np.array_equal(out.download(nbytes), ref_out.ravel()))
 
