@@ -1103,7 +1103,8 @@ def gb300_arm(args, dist):
                                f"target_ratio {args.target:g}, archive resident in HBM",
                    "volume": list(dims), "target_ratio": args.target, "q0": q0, "archive_bytes": len(data),
                    "l2": "flushed between timed steps (512 MiB device write)", "parallelism": f"replicas{dist.world}"},
-        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": nbytes},
+        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": nbytes,
+                "step_ms": [round(t * 1e3, 3) for t in e2e_t]},
         "gpu_launches": launches,
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": dram_traffic(dom, st_["units"] / max(1, st_["launches"])),

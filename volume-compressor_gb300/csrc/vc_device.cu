@@ -73,7 +73,7 @@ static void ctx_free(void *p) {
     if (c->wpin) cudaFreeHost(c->wpin);
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     if (c->copy_stream) {
-        for (int i = 0; i < 16; ++i) cudaEventDestroy(c->chunk_ev[i]);
+        for (int i = 0; i < VCD_SLABS; ++i) cudaEventDestroy(c->chunk_ev[i]);
         cudaStreamDestroy(c->copy_stream);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -194,24 +194,43 @@ cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out) {
 
 // ---------------------------------------------------------------- archive residency
 
-extern "C" int vcd_upload_archive(vcd_archive **out, const uint8_t *buf, size_t len, const vcd_atom *atoms,
-                                  uint64_t n_atoms, const vcd_dq *dq, int nlod) {
+// Residency in two steps, so that the copy of the archive bytes runs while the
+// host resolves the atom table: begin allocates and starts the copy on the
+// calling thread's stream, finish uploads the table and waits for both.
+extern "C" int vcd_upload_begin(vcd_archive **out, const uint8_t *buf, size_t len) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
     vcd_archive *d = (vcd_archive *)calloc(1, sizeof(vcd_archive));
+    if (!d) return 3;
     cudaError_t e;
     if ((e = cudaMalloc(&d->arc, len + 16)) != cudaSuccess ||
-        (e = cudaMemcpy(d->arc, buf, len, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemset(d->arc + len, 0, 16)) != cudaSuccess ||
-        (e = cudaMalloc(&d->atoms, (n_atoms ? n_atoms : 1) * sizeof(vcd_atom))) != cudaSuccess ||
-        (e = cudaMemcpy(d->atoms, atoms, n_atoms * sizeof(vcd_atom), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMalloc(&d->dq, nlod * sizeof(vcd_dq))) != cudaSuccess ||
-        (e = cudaMemcpy(d->dq, dq, nlod * sizeof(vcd_dq), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        (e = cudaMemcpyAsync(d->arc, buf, len, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d->arc + len, 0, 16, c->stream)) != cudaSuccess) {
         vcd_set_error("archive upload", e);
+        cudaStreamSynchronize(c->stream);
         vcd_free_archive(d);
         return vcd_status_of(e);
     }
     d->len = len;
-    d->nlod = nlod;
     *out = d;
+    return 0;
+}
+
+extern "C" int vcd_upload_finish(vcd_archive *d, const vcd_atom *atoms, uint64_t n_atoms, const vcd_dq *dq, int nlod) {
+    vcd_ctx *c = vcd_thread_ctx();
+    if (!c) return 4;
+    cudaError_t e;
+    if ((e = cudaMalloc(&d->atoms, (n_atoms ? n_atoms : 1) * sizeof(vcd_atom))) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d->atoms, atoms, n_atoms * sizeof(vcd_atom), cudaMemcpyHostToDevice, c->stream)) !=
+            cudaSuccess ||
+        (e = cudaMalloc(&d->dq, nlod * sizeof(vcd_dq))) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d->dq, dq, nlod * sizeof(vcd_dq), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+        vcd_set_error("archive upload", e);
+        cudaStreamSynchronize(c->stream);
+        return vcd_status_of(e);
+    }
+    d->nlod = nlod;
     return 0;
 }
 
@@ -279,7 +298,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     StageEvents ev;
     memcpy(ev.ev, c->ev, sizeof ev.ev);
     uint64_t ctl_h[2] = {0xFFFFFFFFull, 0};
-    // Large outputs to pinned host memory: the inverse transform runs in up to 16
+    // Large outputs to pinned host memory: the inverse transform runs in up to 32
     // slabs of atom layers and each finished slab is copied out on a second stream while
     // the next one is transformed. The range decode finishes first, so a stream
     // with a malformed atom is known before any byte reaches the caller.
@@ -296,7 +315,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
                 c->copy_stream = NULL;
                 piped = false;
             } else {
-                for (int i = 0; i < 16; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
+                for (int i = 0; i < VCD_SLABS; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
             }
         }
     }
@@ -313,7 +332,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
             piped = false;
         } else {
             const uint64_t plane = (uint64_t)J.ox * J.oy;
-            const uint64_t per = (layers + 15) / 16;
+            const uint64_t per = (layers + VCD_SLABS - 1) / VCD_SLABS;
             int k = 0;
             for (uint64_t l0 = 0; l0 < layers; l0 += per, ++k) {
                 const uint64_t l1 = l0 + per < layers ? l0 + per : layers;

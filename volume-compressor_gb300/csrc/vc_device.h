@@ -15,6 +15,8 @@ enum {
     VCD_NBUF
 };
 
+constexpr int VCD_SLABS = 32;   // copy-out slabs of a large host-output decode
+
 struct vcd_ctx {
     cudaStream_t stream;
     void *buf[VCD_NBUF];
@@ -29,7 +31,7 @@ struct vcd_ctx {
     unsigned char batch_key[512];   // kernel parameters + shape + grid capacity the graph was captured with
     // copy-out overlapped with the inverse transform (created on first use)
     cudaStream_t copy_stream;
-    cudaEvent_t chunk_ev[16];
+    cudaEvent_t chunk_ev[VCD_SLABS];
     // streamed decode: pinned staging filled by the read callback, copied to VCD_BUF_STG
     uint8_t *stage_host;
     size_t stage_cap;

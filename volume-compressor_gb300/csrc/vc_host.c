@@ -371,6 +371,10 @@ static int make_resident(vc_archive *a) {
     int rc = -1;
     if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); goto done; }
     if (!a->buf && pull_whole(a) != 0) { pthread_mutex_unlock(&a->mu); return -1; }
+    if (vcd_upload_begin(&a->dev, a->buf, a->len) != 0) {   // the copy runs during the walk below
+        report("archive upload failed: %s", vcd_last_error());
+        goto done;
+    }
     uint64_t total = 0;
     for (int l = 0; l < a->nlod; ++l) {
         vc_dims d = lod_dims_of(a->d0, l);
@@ -405,12 +409,16 @@ static int make_resident(vc_archive *a) {
                             }
                 }
     }
-    if (vcd_upload_archive(&a->dev, a->buf, a->len, a->atoms, total, dq, a->nlod) != 0) {
+    if (vcd_upload_finish(a->dev, a->atoms, total, dq, a->nlod) != 0) {
         report("archive upload failed: %s", vcd_last_error());
         goto done;
     }
     rc = 0;
 done:
+    if (rc != 0 && a->dev) {
+        vcd_free_archive(a->dev);   // also waits for a copy still in flight
+        a->dev = NULL;
+    }
     a->resident = rc == 0 ? 1 : -1;
     pthread_mutex_unlock(&a->mu);
     return rc;

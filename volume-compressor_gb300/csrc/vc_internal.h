@@ -90,8 +90,10 @@ typedef struct vcd_archive vcd_archive;   // device residency of one archive
 // ---- device layer (vc_device.cu) ------------------------------------------
 int  vcd_init(void);                        // 0 ok; -1 no usable device
 const char *vcd_last_error(void);
-int  vcd_upload_archive(vcd_archive **out, const uint8_t *buf, size_t len, const vcd_atom *atoms,
-                        uint64_t n_atoms, const vcd_dq *dq /*nlod*/, int nlod);
+// residency: begin starts the copy of the archive bytes, finish adds the atom
+// table and the dequantisation tables and waits (the caller frees on failure)
+int  vcd_upload_begin(vcd_archive **out, const uint8_t *buf, size_t len);
+int  vcd_upload_finish(vcd_archive *d, const vcd_atom *atoms, uint64_t n_atoms, const vcd_dq *dq /*nlod*/, int nlod);
 void vcd_free_archive(vcd_archive *d);
 // decode into a device buffer (out_dev, box bytes) or, when out_dev is NULL, into
 // the host buffer out_host (box raster); returns 0 or a vc_status
