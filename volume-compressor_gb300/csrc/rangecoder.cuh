@@ -312,6 +312,25 @@ struct RcEnc {
 #pragma unroll 1
         for (int i = 0; i < 5; ++i) shift_low();
     }
+    // shift_low for the lanes with ren, the others unchanged, without a branch
+    // around the common case: a byte leaves (cache + carry) unless the top byte
+    // is 0xFF without carry; the 0xFF bytes held back before it (pending - 1 of
+    // them, rarely any) follow as 0xFF + carry.
+    __device__ __forceinline__ void shift_low_if(bool ren) {
+        if (!WRITE) { nbytes += ren ? 1u : 0u; return; }
+        const uint32_t hi = (uint32_t)(low >> 32);
+        const bool emit = ren && (hi != 0u || low < 0xFF000000ull);
+        if (emit && nbytes < cap) out[nbytes] = (uint8_t)(cache + hi);
+        if (emit && pending > 1u) {
+            const uint8_t fill = (uint8_t)(0xFFu + hi);
+            for (uint32_t j = 1; j < pending; ++j)
+                if (nbytes + j < cap) out[nbytes + j] = fill;
+        }
+        nbytes = emit ? nbytes + pending : nbytes;
+        cache = emit ? (uint32_t)(low >> 24) & 0xFFu : cache;
+        pending = ren ? (emit ? 1u : pending + 1u) : pending;
+        low = ren ? (low << 8) & 0xFFFFFFFFull : low;
+    }
 };
 
 // ---------------------------------------------------------------- lockstep encoder
@@ -324,11 +343,7 @@ __device__ __forceinline__ void enc_ctx(bool on, bool bit, RcEnc<WRITE> &e, uint
     const uint32_t nrange = bit ? e.range - r0 : r0;
     const uint32_t nprob = rc_adapt(prob, bit);
     const bool ren = on && nrange < kTop;
-    if (WRITE) {
-        if (ren) e.shift_low();
-    } else {
-        e.nbytes += ren ? 1u : 0u;
-    }
+    e.shift_low_if(ren);
     e.range = on ? (ren ? nrange << 8 : nrange) : e.range;
     prob = on ? nprob : prob;
 }
@@ -338,11 +353,7 @@ __device__ __forceinline__ void enc_byp(bool on, bool bit, RcEnc<WRITE> &e) {
     const uint32_t r0 = e.range >> 1;
     if (WRITE && on && bit) e.low += r0;
     const bool ren = on && r0 < kTop;
-    if (WRITE) {
-        if (ren) e.shift_low();
-    } else {
-        e.nbytes += ren ? 1u : 0u;
-    }
+    e.shift_low_if(ren);
     e.range = on ? (ren ? r0 << 8 : r0) : e.range;
 }
 
