@@ -44,11 +44,23 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
                 T[tile_idx(r)] = dequant((int16_t)lv, r, dqs, dqb, alt);
             });
     } else {
+        // batches of kB entries per thread: every list load of a batch is issued
+        // before the first scan lookup, and every lookup before the first store,
+        // so a batch waits for one memory latency instead of one per entry
+        constexpr uint32_t kB = 16;
         const uint32_t n = c & kEntMask;
-        for (uint32_t i = tid; i < n; i += NT) {
-            const uint32_t w = src[i];
-            const uint32_t r = __ldg(scan + (w & 0xFFFFu));
-            T[tile_idx(r)] = dequant((int16_t)(w >> 16), r, dqs, dqb, alt);
+        for (uint32_t i0 = 0; i0 < n; i0 += kB * NT) {
+            uint32_t w[kB], r[kB];
+#pragma unroll
+            for (uint32_t j = 0; j < kB; ++j) {
+                const uint32_t i = i0 + j * NT + tid;
+                w[j] = i < n ? __ldg(src + i) : 0u;
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < kB; ++j) r[j] = __ldg(scan + (w[j] & 0xFFFFu));
+#pragma unroll
+            for (uint32_t j = 0; j < kB; ++j)
+                if (i0 + j * NT + tid < n) T[tile_idx(r[j])] = dequant((int16_t)(w[j] >> 16), r[j], dqs, dqb, alt);
         }
     }
     __syncthreads();
