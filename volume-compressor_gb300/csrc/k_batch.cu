@@ -235,13 +235,14 @@ __global__ void __launch_bounds__(NT, 1) k_idct_batch_imma(BatchJob J) {
 
 static void launch_rc(const BatchJob &J, int num_sms, uint32_t max_ua, cudaStream_t s) {
     // warps for the widest case up to max_ua atoms: one per atom while the
-    // policy keeps atoms one per warp, else one per 32 atoms; capped at a full
-    // device (the kernel loops)
+    // policy keeps atoms one per warp, else the k warps per sub-partition of
+    // rc_lanes_for (k grows with the atom count); capped at a full device (the
+    // kernel loops)
     const uint64_t slots = 4ull * (uint64_t)num_sms;
     const uint64_t scalar = (uint64_t)J.rc_scalar_warps * slots;
     uint64_t warps = max_ua < scalar ? max_ua : scalar;
-    const uint64_t packed = ((uint64_t)max_ua + 31) / 32;
-    if (packed > warps) warps = packed;
+    const uint64_t packed = ((uint64_t)max_ua + 32 * slots - 1) / (32 * slots) * slots;
+    if (max_ua > scalar && packed > warps) warps = packed;
     const uint64_t cap = (uint64_t)num_sms * (2048 / kRcBatchThreads) * (kRcBatchThreads / 32);
     if (warps > cap) warps = cap;
     if (warps < 1) warps = 1;

@@ -86,14 +86,17 @@ struct BatchShape {              // tunables the autotuner chooses among
 // runs them in lockstep, which costs more decision steps per atom but issues
 // each instruction for all of them. One atom per warp while that makes at most
 // `scalar_warps` warps per SM sub-partition (4 per SM; measured on GB300, the
-// scalar decoder wins up to about 16 per sub-partition), else the smallest
-// power of two that keeps to about one warp per sub-partition, at most 32.
+// scalar decoder wins up to about 16 per sub-partition). Otherwise the fewest
+// warps per sub-partition k that keep a warp at 32 atoms or fewer, and the
+// atoms spread evenly over k warps per sub-partition: for 32,768 atoms on 152
+// SMs that is 27 atoms in 1,214 warps (at most 2 per sub-partition) rather than
+// 32 in 1,024 (2 on 416 sub-partitions, 1 on the rest), 3 % faster measured.
 __host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms, uint32_t scalar_warps) {
     const uint64_t slots = 4ull * sms;
     if (n_atoms <= (uint64_t)scalar_warps * slots) return 1;
-    uint32_t g = 2;
-    while (g < 32 && (uint64_t)g * slots < n_atoms) g <<= 1;
-    return g;
+    const uint64_t k = (n_atoms + 32 * slots - 1) / (32 * slots);
+    const uint64_t g = (n_atoms + k * slots - 1) / (k * slots);
+    return g < 2 ? 2u : (uint32_t)g;
 }
 constexpr uint32_t kRcScalarWarpsDefault = 16;
 // policy of the plain decode path (vcg_set_rc_scalar_warps)
