@@ -1,5 +1,5 @@
 // Shared pieces of the inverse-transform kernels (device): level scatter into a
-// swizzled shared-memory tile, dequantisation, inverse passes along x and y per
+// padded shared-memory tile, dequantisation, inverse passes along x and y per
 // slab, the pass along z per column, and the cropped store into a box raster.
 #pragma once
 #include <stdint.h>
@@ -10,8 +10,17 @@
 
 namespace vcg {
 
-__device__ __forceinline__ int tile_idx(uint32_t r) {   // raster (kz,ky,kx) -> swizzled slab slot
-    return (int)((r >> 10) << 10) | swz((int)((r >> 5) & 31u), (int)(r & 31u));
+// Tile layout: 32 slabs of 32 rows, a row pitch of 33 ints, so a warp that
+// reads one row (lane = column), one column (lane = row) or one (y, x) line
+// across slabs (lane = x) hits 32 distinct banks, and every address in the
+// unrolled passes is a base register plus a constant.
+constexpr int kRowPitch = 33;
+constexpr int kSlabPitch = 32 * kRowPitch;
+constexpr int kTileInts = 32 * kSlabPitch;
+constexpr size_t kTileBytes = (size_t)kTileInts * sizeof(int32_t);
+
+__device__ __forceinline__ int tile_idx(uint32_t r) {   // raster (kz,ky,kx) -> tile slot
+    return (int)(r >> 10) * kSlabPitch + (int)((r >> 5) & 31u) * kRowPitch + (int)(r & 31u);
 }
 
 // dequantised coefficient of raw level l at raster r (src/vc/vc.c:327-338, i32 wrap)
@@ -25,7 +34,7 @@ __device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t 
 }
 
 // Tile of one PRESENT atom after the inverse passes along x and y: levels
-// dequantised as they are scattered into T (32 slabs x swizzled 32x32, i32;
+// dequantised as they are scattered into T (32 slabs x padded 32x32, i32;
 // only the nonzero levels are touched), then one warp per slab (lane per
 // line). Ends with a barrier.
 template <int NT>
@@ -34,7 +43,7 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
                                              const int32_t *dqs, const int32_t *dqb, const uint32_t *alt) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int4 *T4 = reinterpret_cast<int4 *>(T);
-    for (int i = tid; i < 32768 / 4; i += NT) T4[i] = make_int4(0, 0, 0, 0);
+    for (int i = tid; i < kTileInts / 4; i += NT) T4[i] = make_int4(0, 0, 0, 0);
     __syncthreads();
     if (c & kEntOverflow) {
         // slow path for streams whose list exceeded its capacity
@@ -65,25 +74,26 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
     }
     __syncthreads();
     for (int kz = warp; kz < 32; kz += NT / 32) {
-        int32_t *S = T + kz * 1024;
+        int32_t *S = T + kz * kSlabPitch;
+        int32_t *row = S + lane * kRowPitch, *col = S + lane;
         int32_t v[32], o[32];
         int any = 0;
 #pragma unroll
         for (int kx = 0; kx < 32; ++kx) {
-            v[kx] = S[swz(lane, kx)];
+            v[kx] = row[kx];
             any |= v[kx];
         }
         if (__any_sync(0xFFFFFFFFu, any)) {   // an all-zero slab stays zero
             idct32_line(v, o);
 #pragma unroll
-            for (int x = 0; x < 32; ++x) S[swz(lane, x)] = o[x];
+            for (int x = 0; x < 32; ++x) row[x] = o[x];
             __syncwarp();
 #pragma unroll
-            for (int ky = 0; ky < 32; ++ky) v[ky] = S[swz(ky, lane)];
+            for (int ky = 0; ky < 32; ++ky) v[ky] = col[ky * kRowPitch];
             idct32_line(v, o);
             __syncwarp();
 #pragma unroll
-            for (int y = 0; y < 32; ++y) S[swz(y, lane)] = o[y];
+            for (int y = 0; y < 32; ++y) col[y * kRowPitch] = o[y];
         }
         __syncwarp();
     }
@@ -92,9 +102,10 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
 
 // Pass along z for column (y, x = lane): voxel values before +dc.
 __device__ __forceinline__ void idct_col_z(const int32_t *T, int y, int lane, int32_t (&o)[32]) {
+    const int32_t *c = T + y * kRowPitch + lane;
     int32_t v[32];
 #pragma unroll
-    for (int kz = 0; kz < 32; ++kz) v[kz] = T[kz * 1024 + swz(y, lane)];
+    for (int kz = 0; kz < 32; ++kz) v[kz] = c[kz * kSlabPitch];
     idct32_line(v, o);
 }
 

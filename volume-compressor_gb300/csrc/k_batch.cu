@@ -14,7 +14,7 @@
 
 namespace vcg {
 
-constexpr size_t kTileSmem = 32768 * sizeof(int32_t);
+constexpr size_t kTileSmem = kTileBytes;   // the butterfly's padded tile (idct_tile.cuh)
 
 // Persistent over the batch's distinct atoms (their number is read from device
 // memory): G atoms per warp by rc_lanes_for, scalar decoder for G = 1, lockstep
@@ -87,7 +87,7 @@ __device__ __forceinline__ void zero_all(const BatchJob &J, const UAtom &a) {
     }
 }
 
-// Butterfly inverse transform of distinct atom u (T: 128 KiB of shared memory),
+// Butterfly inverse transform of distinct atom u (T: the 132 KiB padded tile),
 // cropped into every box it overlaps. Ends with a barrier.
 template <int NT>
 __device__ __forceinline__ void bf_atom_to_boxes(int32_t *T, const BatchJob &J, const UAtom &a, uint32_t u,

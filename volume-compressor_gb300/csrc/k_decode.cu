@@ -24,7 +24,7 @@
 namespace vcg {
 
 constexpr int kIdctThreads = 512;   // 16 warps per atom (measured faster than 8 on GB300)
-constexpr size_t kIdctSmem = 32768 * sizeof(int32_t);
+constexpr size_t kIdctSmem = kTileBytes;
 
 __global__ void k_caps(DecodeJob J) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -137,7 +137,7 @@ static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s) {
 }
 
 __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
-    extern __shared__ int32_t T[];   // 32 slabs x swizzled 32x32
+    extern __shared__ int32_t T[];   // 32 slabs x padded 32x32 (idct_tile.cuh)
     __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
     __shared__ uint32_t alt[1024];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
