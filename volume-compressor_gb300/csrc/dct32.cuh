@@ -119,9 +119,18 @@ __device__ __forceinline__ void fdct32_line(const int32_t (&v)[32], int32_t (&o)
     o[16] = rnd14(cmat(16, 0) * s4[0] + cmat(16, 1) * s4[1]);
 }
 
-// Swizzled 32x32 i32 tile in shared memory: element (r, c) lives at
-// r*32 + ((c + r) & 31), so a warp touching one row (lane = column) or one
-// column (lane = row) hits 32 distinct banks.
-__device__ __forceinline__ int swz(int r, int c) { return (r << 5) | ((c + r) & 31); }
+// Atom tile in shared memory (i32): 32 slabs of 32 rows with a row pitch of 33
+// ints, element (z, y, x) at z*kSlabPitch + y*kRowPitch + x. A warp that
+// touches one row (lane = x), one column (lane = y) or one (y, x) line across
+// slabs (lane = x) hits 32 distinct banks, and in unrolled loops every address
+// is a base register plus a constant.
+constexpr int kRowPitch = 33;
+constexpr int kSlabPitch = 32 * kRowPitch;
+constexpr int kTileInts = 32 * kSlabPitch;
+constexpr size_t kTileBytes = (size_t)kTileInts * sizeof(int32_t);
+
+__host__ __device__ __forceinline__ int tile_idx(uint32_t r) {   // raster (z, y, x) -> tile slot
+    return (int)(r >> 10) * kSlabPitch + (int)((r >> 5) & 31u) * kRowPitch + (int)(r & 31u);
+}
 
 }  // namespace vcg

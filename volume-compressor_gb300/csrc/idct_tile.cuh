@@ -10,19 +10,6 @@
 
 namespace vcg {
 
-// Tile layout: 32 slabs of 32 rows, a row pitch of 33 ints, so a warp that
-// reads one row (lane = column), one column (lane = row) or one (y, x) line
-// across slabs (lane = x) hits 32 distinct banks, and every address in the
-// unrolled passes is a base register plus a constant.
-constexpr int kRowPitch = 33;
-constexpr int kSlabPitch = 32 * kRowPitch;
-constexpr int kTileInts = 32 * kSlabPitch;
-constexpr size_t kTileBytes = (size_t)kTileInts * sizeof(int32_t);
-
-__device__ __forceinline__ int tile_idx(uint32_t r) {   // raster (kz,ky,kx) -> tile slot
-    return (int)(r >> 10) * kSlabPitch + (int)((r >> 5) & 31u) * kRowPitch + (int)(r & 31u);
-}
-
 // dequantised coefficient of raw level l at raster r (src/vc/vc.c:327-338, i32 wrap)
 __device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t *dqs, const int32_t *dqb,
                                            const uint32_t *alt) {

@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(NT, 1) k_idct_batch(BatchJob J) {
 // values leave the three-piece range take the butterfly, so every result is
 // the reference's.
 constexpr size_t kImmaSmem = 2 * 3 * 32768;   // two buffers of three piece planes
+static_assert(kImmaSmem >= kTileBytes, "an atom redone with the butterfly reuses the planes as its tile");
 
 template <int NT>
 __global__ void __launch_bounds__(NT, 1) k_idct_batch_imma(BatchJob J) {

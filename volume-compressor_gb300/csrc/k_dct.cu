@@ -51,7 +51,6 @@ struct DctJob {
 };
 
 constexpr int kDctThreads = 256;
-constexpr size_t kTileBytes = 32768 * sizeof(int32_t);
 
 __device__ __forceinline__ void atom_xyz(const DctJob &J, uint64_t a, uint64_t &bx, uint64_t &by, uint64_t &bz) {
     bx = (a % J.ax) * 32;
@@ -101,8 +100,8 @@ __device__ __forceinline__ int32_t inv_centre(const DctJob &J, uint64_t a) {
 }
 
 // ------------------------------------------------------------------ butterfly
-// One atom through the three passes with T as a 32 slabs x swizzled 32x32 i32
-// tile (element (z, y, x) at z*1024 + swz(y, x)): x and y per slab (warp per
+// One atom through the three passes with T as the padded 32 slabs x 32x32 i32
+// tile of dct32.cuh: x and y per slab (warp per
 // slab, lane per line), then z per column (thread per column) straight to the
 // output. Starts and ends with the CTA converged.
 template <bool INV>
@@ -121,7 +120,7 @@ __device__ void bf_atom(int32_t *T, const DctJob &J, uint64_t a) {
             const uint32_t ws[4] = {w[k].x, w[k].y, w[k].z, w[k].w};
 #pragma unroll
             for (int b = 0; b < 16; ++b)
-                T[z * 1024 + swz(y, x0 + b)] = (int32_t)((ws[b >> 2] >> (8 * (b & 3))) & 0xFFu) - cen;
+                T[z * kSlabPitch + y * kRowPitch + x0 + b] = (int32_t)((ws[b >> 2] >> (8 * (b & 3))) & 0xFFu) - cen;
         }
     } else {
         cen = inv_centre(J, a);
@@ -129,27 +128,29 @@ __device__ void bf_atom(int32_t *T, const DctJob &J, uint64_t a) {
         for (int i = tid; i < 8192; i += kDctThreads) {
             const int4 w = src[i];
             const int z = i >> 8, y = (i >> 3) & 31, x = (i & 7) * 4;
-            T[z * 1024 + swz(y, x)] = w.x;
-            T[z * 1024 + swz(y, x + 1)] = w.y;
-            T[z * 1024 + swz(y, x + 2)] = w.z;
-            T[z * 1024 + swz(y, x + 3)] = w.w;
+            int32_t *d = T + z * kSlabPitch + y * kRowPitch + x;
+            d[0] = w.x;
+            d[1] = w.y;
+            d[2] = w.z;
+            d[3] = w.w;
         }
     }
     __syncthreads();
     for (int z = warp; z < 32; z += kDctThreads / 32) {
-        int32_t *S = T + z * 1024;
+        int32_t *S = T + z * kSlabPitch;
+        int32_t *row = S + lane * kRowPitch, *col = S + lane;
         int32_t v[32], o[32];
 #pragma unroll
-        for (int x = 0; x < 32; ++x) v[x] = S[swz(lane, x)];
+        for (int x = 0; x < 32; ++x) v[x] = row[x];
         if (INV) idct32_line(v, o); else fdct32_line(v, o);
 #pragma unroll
-        for (int x = 0; x < 32; ++x) S[swz(lane, x)] = o[x];
+        for (int x = 0; x < 32; ++x) row[x] = o[x];
         __syncwarp();
 #pragma unroll
-        for (int y = 0; y < 32; ++y) v[y] = S[swz(y, lane)];
+        for (int y = 0; y < 32; ++y) v[y] = col[y * kRowPitch];
         if (INV) idct32_line(v, o); else fdct32_line(v, o);
 #pragma unroll
-        for (int y = 0; y < 32; ++y) S[swz(y, lane)] = o[y];
+        for (int y = 0; y < 32; ++y) col[y * kRowPitch] = o[y];
         __syncwarp();
     }
     __syncthreads();
@@ -157,7 +158,7 @@ __device__ void bf_atom(int32_t *T, const DctJob &J, uint64_t a) {
         const int y = c >> 5, x = c & 31;
         int32_t v[32], o[32];
 #pragma unroll
-        for (int z = 0; z < 32; ++z) v[z] = T[z * 1024 + swz(y, x)];
+        for (int z = 0; z < 32; ++z) v[z] = T[z * kSlabPitch + y * kRowPitch + x];
         if (INV) {
             idct32_line(v, o);
 #pragma unroll
@@ -325,7 +326,10 @@ static vc_status dct_run(const void *in, void *out, uint8_t *dc, vc_dims dims, i
         name = inverse ? "dct_inverse_butterfly" : "dct_forward_butterfly";
     } else {
         static bool attr = false;
-        const size_t fwd_smem = 2 * 2 * 32768, inv_smem = 2 * 3 * 32768;
+        // piece planes; an atom redone with the butterfly reuses them as its tile
+        const size_t planes_fwd = 2 * 2 * 32768, planes_inv = 2 * 3 * 32768;
+        const size_t fwd_smem = planes_fwd > kTileBytes ? planes_fwd : kTileBytes;
+        const size_t inv_smem = planes_inv > kTileBytes ? planes_inv : kTileBytes;
         if (!attr) {
             cudaFuncSetAttribute(k_dct_imma<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem);
             cudaFuncSetAttribute(k_dct_imma<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)inv_smem);

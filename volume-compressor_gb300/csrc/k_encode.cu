@@ -22,7 +22,7 @@
 namespace vcg {
 
 constexpr int kFwdThreads = 256;
-constexpr size_t kFwdSmem = 32768 * sizeof(int32_t) + 32768 * sizeof(int16_t);
+constexpr size_t kFwdSmem = kTileBytes + 32768 * sizeof(int16_t);
 
 // 32 voxels of row (z, y) of atom (az, ay, ax), zero outside the volume, packed
 // little-endian into 8 words.
@@ -106,8 +106,8 @@ __device__ __forceinline__ uint32_t quant_compact(Coef &&coef, const uint16_t *s
 
 __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
     extern __shared__ int32_t smem[];
-    int32_t *T = smem;                                          // 32 slabs x swizzled 32x32
-    int16_t *L = reinterpret_cast<int16_t *>(smem + 32768);     // levels in scan order
+    int32_t *T = smem;                                          // the padded atom tile (dct32.cuh)
+    int16_t *L = reinterpret_cast<int16_t *>(smem + kTileInts); // levels in scan order
     __shared__ float qdz[VCD_NCLASS], qrr[VCD_NCLASS];
     __shared__ uint32_t alt[1024];
     __shared__ uint32_t red[32];
@@ -181,34 +181,35 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
 #pragma unroll
                 for (int i = 0; i < 32; ++i) v[i] = (int32_t)((w[j][i >> 2] >> (8 * (i & 3))) & 0xFFu) - dc;
                 fdct32_line(v, o);
-                int32_t *S = T + (r >> 5) * 1024;
+                int32_t *S = T + (r >> 5) * kSlabPitch + (r & 31) * kRowPitch;
 #pragma unroll
-                for (int k = 0; k < 32; ++k) S[swz(r & 31, k)] = o[k];
+                for (int k = 0; k < 32; ++k) S[k] = o[k];
             }
             __syncthreads();
             // pass along y, warp per z-slab, lane per column kx
             for (int z = warp; z < 32; z += kFwdThreads / 32) {
-                int32_t *S = T + z * 1024;
+                int32_t *S = T + z * kSlabPitch + lane;
                 int32_t v[32], o[32];
 #pragma unroll
-                for (int y = 0; y < 32; ++y) v[y] = S[swz(y, lane)];
+                for (int y = 0; y < 32; ++y) v[y] = S[y * kRowPitch];
                 fdct32_line(v, o);
 #pragma unroll
-                for (int k = 0; k < 32; ++k) S[swz(k, lane)] = o[k];
+                for (int k = 0; k < 32; ++k) S[k * kRowPitch] = o[k];
             }
             __syncthreads();
             // pass along z per column (ky, kx = lane), coefficients back in place
             for (int ky = warp; ky < 32; ky += kFwdThreads / 32) {
+                int32_t *C = T + ky * kRowPitch + lane;
                 int32_t v[32], o[32];
 #pragma unroll
-                for (int z = 0; z < 32; ++z) v[z] = T[z * 1024 + swz(ky, lane)];
+                for (int z = 0; z < 32; ++z) v[z] = C[z * kSlabPitch];
                 fdct32_line(v, o);
 #pragma unroll
-                for (int kz = 0; kz < 32; ++kz) T[kz * 1024 + swz(ky, lane)] = o[kz];
+                for (int kz = 0; kz < 32; ++kz) C[kz * kSlabPitch] = o[kz];
             }
             __syncthreads();
             auto tile = [&](uint32_t p, uint32_t r) {
-                const int32_t cf = T[((r >> 10) << 10) | swz((int)((r >> 5) & 31u), (int)(r & 31u))];
+                const int32_t cf = T[tile_idx(r)];
                 if (cached) cptr[p] = cf;   // kept in scan order
                 return cf;
             };
