@@ -42,46 +42,67 @@ __device__ __forceinline__ void load_row(const uint8_t *vol, uint32_t nx, uint32
     for (uint32_t i = 0; i < cnt; ++i) w[i >> 2] |= (uint32_t)__ldg(p + i) << (8 * (i & 3));
 }
 
-// Dead-zone quantiser of coefficient cf at raster r, as the release build
-// evaluates it (src/vc/vc.c:293-306): step class from the frequency and the
-// alternate-step bit, level = trunc((|cf| - dz) r' + 1) for |cf| >= dz, clamped.
-__device__ __forceinline__ int32_t quant_level(int32_t cf, uint32_t r, const float *qdz, const float *qrr,
-                                               const uint32_t *alt) {
+// Quantiser class of raster r: its frequency, + 94 where the alternate step
+// applies (src/vc/vc.c:273-279, 293-306).
+__device__ __forceinline__ uint32_t quant_class(uint32_t r, const uint32_t *alt) {
     const uint32_t f = (r >> 10) + ((r >> 5) & 31u) + (r & 31u);
-    const uint32_t cls = f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
+    return f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
+}
+
+// A coefficient with its class, as the quantiser needs it: |cf| (< 2^17: the
+// transform of 8-bit voxels stays below 46,300) in bits 0-16, the class in bits
+// 17-24, the sign in bit 31. Quantising it needs no scan order or class lookup.
+__device__ __forceinline__ uint32_t coef_pack(int32_t cf, uint32_t r, const uint32_t *alt) {
     const uint32_t mag = cf < 0 ? 0u - (uint32_t)cf : (uint32_t)cf;
-    const float fa = __int2float_rn((int32_t)mag);
+    return mag | (quant_class(r, alt) << 17) | (cf < 0 ? 0x80000000u : 0u);
+}
+
+// Dead-zone quantiser of a packed coefficient, as the release build evaluates
+// it (src/vc/vc.c:293-306): level = trunc((|cf| - dz) r' + 1) for |cf| >= dz,
+// clamped, with the coefficient's sign.
+__device__ __forceinline__ int32_t quant_packed(uint32_t w, const float *qdz, const float *qrr) {
+    const uint32_t cls = (w >> 17) & 0xFFu;
+    const float fa = __int2float_rn((int32_t)(w & 0x1FFFFu));
     int32_t level = 0;
     if (fa >= qdz[cls]) {
         level = __float2int_rz(__fadd_rn(__fmul_rn(__fsub_rn(fa, qdz[cls]), qrr[cls]), 1.0f));
         if (level > 32767) level = 32767;
     }
-    return cf < 0 ? -level : level;
+    return (w >> 31) ? -level : level;
 }
 
 // Quantise one atom in scan order and compact its nonzero levels into the list
 // dst (scan position | level << 16, in scan order); returns the count (every
-// thread). Warp w owns scan positions [4096 w, 4096 w + 4096), 32 at a time, so
-// coefficient reads, level stores and list writes are contiguous per warp:
-// pass 1 quantises (coef(p, r) gives the coefficient of scan position p, raster
-// r), keeps the levels in lv and counts them with warp ballots; pass 2 writes
-// the entries at the warp's offset. NT must be 256.
-template <int NT, class Coef>
-__device__ __forceinline__ uint32_t quant_compact(Coef &&coef, const uint16_t *scan, const float *qdz,
-                                                  const float *qrr, const uint32_t *alt, int16_t *lv,
+// thread). Warp w owns scan positions [4096 w, 4096 w + 4096), 128 at a time,
+// each lane 4 consecutive ones (pk4(p) gives the packed coefficients of scan
+// positions p..p+3): pass 1 quantises, keeps the levels in lv and counts them;
+// pass 2 places each lane's entries after a warp prefix sum of the per-lane
+// counts, skipping groups without a nonzero level. NT must be 256.
+template <int NT, class Pk4>
+__device__ __forceinline__ uint32_t quant_compact(Pk4 &&pk4, const float *qdz, const float *qrr, int16_t *lv,
                                                   uint32_t *wcnt, uint32_t *dst) {
     static_assert(NT == 256, "eight warps of 4096 scan positions");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t p0 = (uint32_t)warp * 4096u;
+    const uint32_t p0 = (uint32_t)warp * 4096u + 4u * (uint32_t)lane;
     uint32_t cnt = 0;
-#pragma unroll 4
-    for (uint32_t i = 0; i < 4096; i += 32) {
-        const uint32_t p = p0 + i + lane;
-        const uint32_t r = __ldg(scan + p);
-        const int32_t level = quant_level(coef(p, r), r, qdz, qrr, alt);
-        lv[p] = (int16_t)level;
-        cnt += __popc(__ballot_sync(0xFFFFFFFFu, level != 0));
+    // groups of kG x 128 positions: every load of a group is issued before the
+    // first level is stored
+    constexpr uint32_t kG = 4;
+#pragma unroll 1
+    for (uint32_t i = 0; i < 4096; i += 128 * kG) {
+        uint4 w[kG];
+#pragma unroll
+        for (uint32_t g = 0; g < kG; ++g) w[g] = pk4(p0 + i + 128 * g);
+#pragma unroll
+        for (uint32_t g = 0; g < kG; ++g) {
+            const int32_t l0 = quant_packed(w[g].x, qdz, qrr), l1 = quant_packed(w[g].y, qdz, qrr);
+            const int32_t l2 = quant_packed(w[g].z, qdz, qrr), l3 = quant_packed(w[g].w, qdz, qrr);
+            *reinterpret_cast<uint2 *>(lv + p0 + i + 128 * g) =
+                make_uint2((uint32_t)(uint16_t)l0 | ((uint32_t)l1 << 16), (uint32_t)(uint16_t)l2 | ((uint32_t)l3 << 16));
+            cnt += (uint32_t)(l0 != 0) + (uint32_t)(l1 != 0) + (uint32_t)(l2 != 0) + (uint32_t)(l3 != 0);
+        }
     }
+    cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
     if (lane == 0) wcnt[warp] = cnt;
     __syncthreads();
     uint32_t base = 0, total = 0;
@@ -91,14 +112,25 @@ __device__ __forceinline__ uint32_t quant_compact(Coef &&coef, const uint16_t *s
         base += w < warp ? v : 0u;
         total += v;
     }
-    const uint32_t below = (1u << lane) - 1u;
 #pragma unroll 4
-    for (uint32_t i = 0; i < 4096; i += 32) {
-        const uint32_t p = p0 + i + lane;
-        const int32_t level = lv[p];
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, level != 0);
-        if (level) dst[base + __popc(m & below)] = p | ((uint32_t)(uint16_t)level << 16);
-        base += __popc(m);
+    for (uint32_t i = 0; i < 4096; i += 128) {
+        const uint32_t p = p0 + i;
+        const uint2 pk = *reinterpret_cast<const uint2 *>(lv + p);
+        if (!__any_sync(0xFFFFFFFFu, (pk.x | pk.y) != 0u)) continue;
+        const uint32_t lw[4] = {pk.x & 0xFFFFu, pk.x >> 16, pk.y & 0xFFFFu, pk.y >> 16};
+        const uint32_t k = (uint32_t)(lw[0] != 0) + (uint32_t)(lw[1] != 0) + (uint32_t)(lw[2] != 0) +
+                           (uint32_t)(lw[3] != 0);
+        uint32_t incl = k;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        uint32_t *d = dst + base + (incl - k);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (lw[j]) *d++ = (p + (uint32_t)j) | (lw[j] << 16);
+        base += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
     __syncthreads();   // lv and wcnt are reused by the next atom
     return total;
@@ -129,7 +161,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
             __syncthreads();
         }
         const bool cached = J.coef && ca < J.coef_n;
-        int32_t *cptr = cached ? J.coef + ca * 32768ull : nullptr;
+        uint32_t *cptr = cached ? J.coef + ca * 32768ull : nullptr;
         uint32_t *dst = J.ent + t * (uint64_t)VCD_MAX_ENTRIES;
         int32_t dc;
         uint32_t total;
@@ -141,8 +173,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
                 continue;
             }
             dc = (int32_t)(dcz & 0xFFu);
-            total = quant_compact<kFwdThreads>([&](uint32_t p, uint32_t) { return __ldcs(cptr + p); }, J.scan, qdz,
-                                               qrr, alt, L, wcnt, dst);
+            total = quant_compact<kFwdThreads>(
+                [&](uint32_t p) { return __ldcs(reinterpret_cast<const uint4 *>(cptr + p)); }, qdz, qrr, L, wcnt, dst);
         } else {
             const uint8_t *vol = J.vol[lod];
             const uint32_t nx = J.dims[lod][0], ny = J.dims[lod][1], nz = J.dims[lod][2];
@@ -208,12 +240,15 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_fwd(FwdJob J) {
                 for (int kz = 0; kz < 32; ++kz) C[kz * kSlabPitch] = o[kz];
             }
             __syncthreads();
-            auto tile = [&](uint32_t p, uint32_t r) {
-                const int32_t cf = T[tile_idx(r)];
-                if (cached) cptr[p] = cf;   // kept in scan order
-                return cf;
+            auto tile = [&](uint32_t p) {
+                const uint2 sc = __ldg(reinterpret_cast<const uint2 *>(J.scan + p));
+                const uint32_t r0 = sc.x & 0xFFFFu, r1 = sc.x >> 16, r2 = sc.y & 0xFFFFu, r3 = sc.y >> 16;
+                const uint4 w = make_uint4(coef_pack(T[tile_idx(r0)], r0, alt), coef_pack(T[tile_idx(r1)], r1, alt),
+                                           coef_pack(T[tile_idx(r2)], r2, alt), coef_pack(T[tile_idx(r3)], r3, alt));
+                if (cached) *reinterpret_cast<uint4 *>(cptr + p) = w;   // kept in scan order
+                return w;
             };
-            total = quant_compact<kFwdThreads>(tile, J.scan, qdz, qrr, alt, L, wcnt, dst);
+            total = quant_compact<kFwdThreads>(tile, qdz, qrr, L, wcnt, dst);
         }
         if (tid == 0) J.meta[t] = total | ((uint32_t)dc << 16);
     }
@@ -226,10 +261,8 @@ constexpr size_t kQuantSmem = 32768 * sizeof(int16_t);
 __global__ void __launch_bounds__(kFwdThreads) k_quant_cached(FwdJob J) {
     extern __shared__ int16_t lv[];
     __shared__ float qdz[VCD_NCLASS], qrr[VCD_NCLASS];
-    __shared__ uint32_t alt[1024];
     __shared__ uint32_t wcnt[kFwdThreads / 32];
     const int tid = threadIdx.x;
-    for (int i = tid; i < 1024; i += kFwdThreads) alt[i] = J.alt_mask[i];
     for (int i = tid; i < VCD_NCLASS; i += kFwdThreads) { qdz[i] = J.q[0].dz[i]; qrr[i] = J.q[0].rr[i]; }
     __syncthreads();
     for (uint64_t t = blockIdx.x; t < J.n_atoms; t += gridDim.x) {
@@ -239,10 +272,10 @@ __global__ void __launch_bounds__(kFwdThreads) k_quant_cached(FwdJob J) {
             if (tid == 0) J.meta[t] = kMetaZero;
             continue;
         }
-        const int32_t *cptr = J.coef + ca * 32768ull;
-        const uint32_t total = quant_compact<kFwdThreads>([&](uint32_t p, uint32_t) { return __ldcs(cptr + p); },
-                                                          J.scan, qdz, qrr, alt, lv, wcnt,
-                                                          J.ent + t * (uint64_t)VCD_MAX_ENTRIES);
+        const uint32_t *cptr = J.coef + ca * 32768ull;
+        const uint32_t total = quant_compact<kFwdThreads>(
+            [&](uint32_t p) { return __ldcs(reinterpret_cast<const uint4 *>(cptr + p)); }, qdz, qrr, lv, wcnt,
+            J.ent + t * (uint64_t)VCD_MAX_ENTRIES);
         if (tid == 0) J.meta[t] = total | ((dcz & 0xFFu) << 16);
     }
 }

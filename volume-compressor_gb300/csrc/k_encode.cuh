@@ -50,10 +50,11 @@ struct FwdJob {
     const uint32_t *alt_mask;
     uint32_t *ent;               // per atom VCD_MAX_ENTRIES slots: scan position | level << 16
     uint32_t *meta;              // per atom
-    // coefficient cache of canonical atoms [0, coef_n): 32768 i32 per atom in
-    // scan order, and dc | kMetaZero per atom; coef_store != 0 fills it, else
-    // atoms below coef_n are quantised from it
-    int32_t *coef;
+    // coefficient cache of canonical atoms [0, coef_n): 32768 packed words per
+    // atom in scan order (coef_pack: magnitude, quantiser class, sign), and
+    // dc | kMetaZero per atom; coef_store != 0 fills it, else atoms below
+    // coef_n are quantised from it
+    uint32_t *coef;
     uint32_t *coef_dc;
     uint64_t coef_n;
     int coef_store;

@@ -40,8 +40,8 @@ struct EncState {
     unsigned long long *red;
     vcd_quant *qtab;          // device, per LOD
     vcd_quant qh;             // host staging
-    // LOD0 forward transform kept across passes (null when it does not fit)
-    int32_t *coef;
+    // LOD0 forward transform kept across passes, packed (null when it does not fit)
+    uint32_t *coef;
     uint32_t *coef_dc;
     uint64_t coef_n;
     bool coef_valid;
@@ -188,7 +188,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
         const size_t cb = (size_t)na0 * 131072 + (size_t)na0 * 4 + 64;
         if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && (c->cap[VCD_BUF_COEF] >= cb || cb <= fr / 2) &&
             vcd_scratch(c, VCD_BUF_COEF, cb, &p) == cudaSuccess) {
-            S.coef = (int32_t *)p;
+            S.coef = (uint32_t *)p;
             S.coef_dc = (uint32_t *)((uint8_t *)p + (size_t)na0 * 131072);
             S.coef_n = na0;
         }
