@@ -280,14 +280,16 @@ __global__ void __launch_bounds__(kFwdThreads) k_quant_cached(FwdJob J) {
     }
 }
 
+// G atoms per warp (lanes 0..G-1; enc_lanes_for). Every lane takes part in the
+// warp-lockstep coder; lanes without a present atom run along inactive.
 template <bool WRITE>
-__global__ void __launch_bounds__(128) k_rc_encode(RcJob J) {
+__global__ void __launch_bounds__(128) k_rc_encode(RcJob J, uint32_t G) {
     __shared__ uint32_t bstart[9];
     if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
     __syncthreads();
-    // every lane takes part in the warp-lockstep coder; lanes without a
-    // present atom run along inactive
-    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t t = lane < G ? w * G + lane : ~0ull;
     const uint32_t meta = t < J.n_atoms ? J.meta[t] : kMetaZero;
     const bool active = !(meta & kMetaZero);
     if (!WRITE && t < J.n_atoms && !active) J.len[t] = 0;
@@ -395,11 +397,24 @@ void launch_fwd(const FwdJob &J, int num_sms, cudaStream_t s) {
     k_fwd<<<(unsigned)grid, kFwdThreads, kFwdSmem, s>>>(J);
 }
 
-void launch_rc_encode(const RcJob &J, bool write, cudaStream_t s) {
+// Atoms per warp of the lockstep encoder: the fewest warps per SM
+// sub-partition k that keep a warp at 32 atoms or fewer, the atoms spread
+// evenly over k warps per sub-partition (as rc_lanes_for, without its
+// one-lane decoder); small batches get one atom per warp.
+static uint32_t enc_lanes_for(uint64_t n, int num_sms) {
+    const uint64_t slots = 4ull * (uint64_t)num_sms;
+    const uint64_t k = (n + 32 * slots - 1) / (32 * slots);
+    const uint64_t g = (n + k * slots - 1) / (k * slots);
+    return g < 1 ? 1u : (uint32_t)g;
+}
+
+void launch_rc_encode(const RcJob &J, bool write, int num_sms, cudaStream_t s) {
     if (!J.n_atoms) return;
-    unsigned nb = (unsigned)((J.n_atoms + 127) / 128);
-    if (write) k_rc_encode<true><<<nb, 128, 0, s>>>(J);
-    else k_rc_encode<false><<<nb, 128, 0, s>>>(J);
+    const uint32_t G = enc_lanes_for(J.n_atoms, num_sms);
+    const uint64_t warps = (J.n_atoms + G - 1) / G;
+    const unsigned nb = (unsigned)((warps + 3) / 4);
+    if (write) k_rc_encode<true><<<nb, 128, 0, s>>>(J, G);
+    else k_rc_encode<false><<<nb, 128, 0, s>>>(J, G);
 }
 
 void launch_consume(const PlaceJob &J, cudaStream_t s) {

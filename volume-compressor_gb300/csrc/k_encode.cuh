@@ -91,7 +91,7 @@ struct PlaceJob {
 void launch_fwd(const FwdJob &J, int num_sms, cudaStream_t s);
 // atoms that are all LOD0 with kept coefficients: quantise and compact only
 void launch_quant_cached(const FwdJob &J, int num_sms, cudaStream_t s);
-void launch_rc_encode(const RcJob &J, bool write, cudaStream_t s);
+void launch_rc_encode(const RcJob &J, bool write, int num_sms, cudaStream_t s);
 void launch_consume(const PlaceJob &J, cudaStream_t s);
 void launch_slots(const PlaceJob &J, cudaStream_t s);
 void launch_gather_dc(const uint32_t *meta, uint64_t n, uint8_t *dc, cudaStream_t s);

@@ -99,7 +99,7 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
             launch_gather_dc(S.meta, n, S.dc + c0, S.c->stream);
         }
         if (prof) cudaEventRecord(S.c->ev[5], S.c->stream);
-        launch_rc_encode(R, write, S.c->stream);
+        launch_rc_encode(R, write, g_dev.num_sms, S.c->stream);
         if (S.coef && c0 < S.coef_n && c0 + n >= S.coef_n) S.coef_valid = true;   // LOD0 transform kept
         if (prof) {
             cudaEventRecord(S.c->ev[1], S.c->stream);
@@ -414,7 +414,7 @@ extern "C" int vcd_encode_segments(const vcd_seg *segs, int nseg, const float *q
             W.arc = dslots;
             W.slot_bytes = kSlot;
             W.len = dlen;
-            launch_rc_encode(W, true, st);
+            launch_rc_encode(W, true, g_dev.num_sms, st);
             if ((e = cudaMemcpyAsync(S.len + c0, dlen, n * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
                 (e = cudaStreamSynchronize(st)) != cudaSuccess)
                 break;
@@ -436,7 +436,7 @@ extern "C" int vcd_encode_segments(const vcd_seg *segs, int nseg, const float *q
                 W.len = nullptr;
                 W.arc = dpack;
                 W.dst_off = doff;
-                launch_rc_encode(W, true, st);
+                launch_rc_encode(W, true, g_dev.num_sms, st);
             }
             if (total + bytes > c->wpin_cap) {   // grow the pinned output, keeping what it holds
                 if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
