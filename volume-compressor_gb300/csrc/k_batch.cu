@@ -87,24 +87,78 @@ __device__ __forceinline__ void zero_all(const BatchJob &J, const UAtom &a) {
     }
 }
 
+// Window of one box in the atom being transformed, staged in shared memory
+// once per atom: the column stores below then need no request loads, crop
+// arithmetic or 64-bit multiplies per row.
+struct BoxStage {
+    uint8_t *ob;       // first voxel of the window
+    uint64_t plane;    // box bytes per z
+    uint32_t ox;       // box bytes per y
+    uint8_t lx0, lx1, ly0, ly1, lz0, lz1, full, pad;   // atom-local window; full: all 32 z
+};
+constexpr uint32_t kBoxStage = 64;   // windows staged per atom; further boxes take BoxWin per row
+
 // Butterfly inverse transform of distinct atom u (T: the 132 KiB padded tile),
-// cropped into every box it overlaps. Ends with a barrier.
+// cropped into every box it overlaps: each row's 32 voxels are clamped once,
+// then stored into every box window. Ends with a barrier.
 template <int NT>
 __device__ __forceinline__ void bf_atom_to_boxes(int32_t *T, const BatchJob &J, const UAtom &a, uint32_t u,
                                                  const vcd_atom &e, uint32_t c, const int32_t *dqs,
                                                  const int32_t *dqb, const uint32_t *alt) {
+    __shared__ BoxStage bs[kBoxStage];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t dc = J.arc[e.off];
+    const uint32_t nb = a.dst_end - a.dst_begin, ns = nb < kBoxStage ? nb : kBoxStage;
+    if ((uint32_t)threadIdx.x < ns) {   // read after idct_tile_xy's first barrier
+        const BoxWin w(J.reqs[J.dst[a.dst_begin + threadIdx.x]], a.ax * 32, a.ay * 32, a.az * 32);
+        BoxStage b;
+        b.ob = w.ob;
+        b.plane = w.ox * w.oy;
+        b.ox = (uint32_t)w.ox;
+        b.lx0 = (uint8_t)w.k.lx0; b.lx1 = (uint8_t)w.k.lx1;
+        b.ly0 = (uint8_t)w.k.ly0; b.ly1 = (uint8_t)w.k.ly1;
+        b.lz0 = (uint8_t)w.k.lz0; b.lz1 = (uint8_t)w.k.lz1;
+        b.full = w.k.lz0 == 0 && w.k.lz1 == 32;
+        b.pad = 0;
+        bs[threadIdx.x] = b;
+    }
     idct_tile_xy<NT>(T, J.arc, e, c, J.ent + J.ent_off[u], J.scan, J.band_start, dqs, dqb, alt);
     for (int y = warp; y < 32; y += NT / 32) {
         int32_t o[32];
         idct_col_z(T, y, lane, o);
-        for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) {
+        uint32_t v[32];
+#pragma unroll
+        for (int z = 0; z < 32; ++z) {
+            const int32_t x = (int32_t)((uint32_t)o[z] + (uint32_t)dc);
+            v[z] = (uint32_t)(x < 0 ? 0 : x > 255 ? 255 : x);
+        }
+        for (uint32_t i = 0; i < ns; ++i) {
+            const BoxStage b = bs[i];
+            if ((uint32_t)y < b.ly0 || (uint32_t)y >= b.ly1 || (uint32_t)lane < b.lx0 || (uint32_t)lane >= b.lx1)
+                continue;
+            uint8_t *p = b.ob + (uint64_t)((uint32_t)y - b.ly0) * b.ox + ((uint32_t)lane - b.lx0);
+            if (b.full) {
+#pragma unroll
+                for (int z = 0; z < 32; ++z) {
+                    *p = (uint8_t)v[z];
+                    p += b.plane;
+                }
+            } else {
+#pragma unroll
+                for (int z = 0; z < 32; ++z) {
+                    if ((uint32_t)z >= b.lz0 && (uint32_t)z < b.lz1) {
+                        *p = (uint8_t)v[z];
+                        p += b.plane;
+                    }
+                }
+            }
+        }
+        for (uint32_t d = a.dst_begin + ns; d < a.dst_end; ++d) {
             const BoxWin w(J.reqs[J.dst[d]], a.ax * 32, a.ay * 32, a.az * 32);
             store_col(w.ob, w.ox, w.oy, w.k, y, lane, o, dc);
         }
     }
-    __syncthreads();
+    __syncthreads();   // the tile and the staged windows are reused by the next atom
 }
 
 template <int NT>
@@ -261,11 +315,13 @@ static void launch_tx(const BatchJob &J, int num_sms, cudaStream_t s) {
     k_idct_batch<NT><<<num_sms, NT, kTileSmem, s>>>(J);
 }
 
-void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s) {
+void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s,
+                  cudaEvent_t mid) {
     BatchJob Jr = J;
     Jr.rc_scalar_warps = (uint32_t)shape.rc_scalar_warps;
     Jr.sms = (uint32_t)num_sms;
     launch_rc(Jr, num_sms, max_ua, s);
+    if (mid) cudaEventRecord(mid, s);
     if (shape.imma) {
         static bool attr = false;
         if (!attr) {

@@ -101,7 +101,9 @@ __host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms,
 constexpr uint32_t kRcScalarWarpsDefault = 16;
 // policy of the plain decode path (vcg_set_rc_scalar_warps)
 uint32_t rc_scalar_warps();
-void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s);
+// mid (optional): recorded between the range decode and the transform
+void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s,
+                  cudaEvent_t mid = nullptr);
 
 void launch_decode(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev);
 // The decode in two halves: list placement + range decode (events ev[0..2]),

@@ -155,20 +155,30 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
         CKB(e, "graph instantiate");
         memcpy(c->batch_key, key, sizeof key);
     }
+    // with per-stage measurement on, the same two kernels run without the graph
+    // and an event between them splits the time
+    const bool prof = vcd_prof_on();
     cudaEventRecord(c->ev[2], st);
-    CKB(cudaGraphLaunch(c->batch_graph, st), "graph launch");
+    if (prof) {
+        launch_batch(J, shape, g_dev.num_sms, max_ua, st, c->ev[5]);
+        CKB(cudaGetLastError(), "batch launch");
+    } else {
+        CKB(cudaGraphLaunch(c->batch_graph, st), "graph launch");
+    }
     cudaEventRecord(c->ev[3], st);
     CKB(cudaMemcpyAsync(req_err, ctl + 4, (size_t)b->n_req * 4, cudaMemcpyDeviceToHost, st), "errors");
     CKB(cudaStreamSynchronize(st), "batch decode");
     CKB(cudaGetLastError(), "batch decode");
     c->last_ms = vcd_elapsed(c->ev[2], c->ev[3]);
-    if (vcd_prof_on()) {
+    if (prof) {
         uint64_t out_bytes = 0;
         for (uint32_t i = 0; i < b->n_req; ++i) {
             const vcd_boxreq &r = b->reqs[i];
             out_bytes += (uint64_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
         }
         vcd_prof_add("batch_decode", c->last_ms, 2, 0, out_bytes, b->n_ua);
+        vcd_prof_add("batch_rc_decode", vcd_elapsed(c->ev[2], c->ev[5]), 1, 0, 0, b->n_ua);
+        vcd_prof_add("batch_transform", vcd_elapsed(c->ev[5], c->ev[3]), 1, 0, out_bytes, b->n_ua);
     }
     if (host_out) {
         void *pin;
