@@ -242,6 +242,18 @@ extern "C" void vcd_free_archive(vcd_archive *d) {
     free(d);
 }
 
+cudaStream_t vcd_side_stream(vcd_ctx *c) {
+    if (!c->copy_stream) {
+        if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            c->copy_stream = NULL;
+            return NULL;
+        }
+        for (int i = 0; i < VCD_SLABS; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
+    }
+    return c->copy_stream;
+}
+
 // ---------------------------------------------------------------- decode
 // One box decode from device bytes `arc` and atom table `atoms` (LOD raster, or
 // box order when box_table). last_ms spans from `t0` (or the first stage event).
@@ -310,14 +322,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
         cudaPointerAttributes pa;
         piped = cudaPointerGetAttributes(&pa, out_host) == cudaSuccess && pa.type == cudaMemoryTypeHost;
         cudaGetLastError();
-        if (piped && !c->copy_stream) {
-            if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
-                c->copy_stream = NULL;
-                piped = false;
-            } else {
-                for (int i = 0; i < VCD_SLABS; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
-            }
-        }
+        if (piped && !vcd_side_stream(c)) piped = false;
     }
     if (piped) {
         launch_decode_front(J, g_dev.num_sms, c->stream, &ev);

@@ -12,6 +12,7 @@ enum {
     VCD_BUF_BEST, VCD_BUF_RED,
     VCD_BUF_BUA, VCD_BUF_BDST, VCD_BUF_BREQ, VCD_BUF_BOFF, VCD_BUF_BCNT, VCD_BUF_BENT, VCD_BUF_BCTL, VCD_BUF_BOUT,
     VCD_BUF_BPIN, VCD_BUF_COEF, VCD_BUF_RPK, VCD_BUF_RPKREC, VCD_BUF_STG, VCD_BUF_WPACK,
+    VCD_BUF_EENT2, VCD_BUF_EMETA2,   // encode: lists and metadata of the coarser LODs (second stream)
     VCD_NBUF
 };
 
@@ -29,7 +30,8 @@ struct vcd_ctx {
     int batch_rc_scalar_warps, batch_tx_threads, batch_imma, batch_forced;
     cudaGraphExec_t batch_graph;
     unsigned char batch_key[512];   // kernel parameters + shape + grid capacity the graph was captured with
-    // copy-out overlapped with the inverse transform (created on first use)
+    // second stream (created on first use, vcd_side_stream): copy-out overlapped
+    // with the inverse transform; the coarser LODs' coder passes beside LOD0's
     cudaStream_t copy_stream;
     cudaEvent_t chunk_ev[VCD_SLABS];
     // streamed decode: pinned staging filled by the read callback, copied to VCD_BUF_STG
@@ -65,5 +67,7 @@ extern vcd_device g_dev;
 vcd_ctx *vcd_thread_ctx(void);
 cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out);
 cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out);
+// the context's second stream and its VCD_SLABS events, created on first use; NULL if that fails
+cudaStream_t vcd_side_stream(vcd_ctx *c);
 void vcd_set_error(const char *what, cudaError_t e);
 int vcd_status_of(cudaError_t e);

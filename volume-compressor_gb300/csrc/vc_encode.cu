@@ -54,10 +54,12 @@ static void set_q(EncState &S, int lod, float q) {
 }
 
 // Forward + coder passes over canonical atoms [a0, a1) (any mix of LODs, each at
-// the q in the device table): size-only (lengths into len and the totals) or
-// writing payloads into the archive. One launch pair per kChunk atoms: a coder
-// launch costs about one atom's serial coding time however many atoms it holds.
-static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
+// the q in the device table) on stream st with list and metadata scratch ent,
+// meta (kChunk atoms): size-only (lengths into len and the totals) or writing
+// payloads into the archive. One launch pair per kChunk atoms: a coder launch
+// costs about one atom's serial coding time however many atoms it holds.
+static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write, cudaStream_t st, uint32_t *ent,
+                     uint32_t *meta) {
     for (uint64_t c0 = a0; c0 < a1; c0 += kChunk) {
         const uint64_t n = a1 - c0 < kChunk ? a1 - c0 : kChunk;
         FwdJob F;
@@ -70,22 +72,22 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
         F.q = S.qtab;
         F.scan = g_dev.tables->scan;
         F.alt_mask = g_dev.tables->alt_mask;
-        F.ent = S.ent;
-        F.meta = S.meta;
+        F.ent = ent;
+        F.meta = meta;
         F.coef = S.coef;
         F.coef_dc = S.coef_dc;
         F.coef_n = S.coef_n;
         F.coef_store = !S.coef_valid;
         const bool from_cache = S.coef && S.coef_valid && c0 + n <= S.coef_n;
         const bool prof = vcd_prof_on();
-        if (prof) cudaEventRecord(S.c->ev[4], S.c->stream);
-        if (from_cache) launch_quant_cached(F, g_dev.num_sms, S.c->stream);
-        else launch_fwd(F, g_dev.num_sms, S.c->stream);
+        if (prof) cudaEventRecord(S.c->ev[4], st);
+        if (from_cache) launch_quant_cached(F, g_dev.num_sms, st);
+        else launch_fwd(F, g_dev.num_sms, st);
         RcJob R;
         memset(&R, 0, sizeof R);
         R.n_atoms = n;
-        R.meta = S.meta;
-        R.ent = S.ent;
+        R.meta = meta;
+        R.ent = ent;
         memcpy(R.band_start, g_dev.band_start, sizeof R.band_start);
         if (!write) {
             R.len = S.len + c0;
@@ -96,13 +98,13 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
             R.pos = S.pos;
             R.canon_first = c0;
             R.lay = S.lay;
-            launch_gather_dc(S.meta, n, S.dc + c0, S.c->stream);
+            launch_gather_dc(meta, n, S.dc + c0, st);
         }
-        if (prof) cudaEventRecord(S.c->ev[5], S.c->stream);
-        launch_rc_encode(R, write, g_dev.num_sms, S.c->stream);
+        if (prof) cudaEventRecord(S.c->ev[5], st);
+        launch_rc_encode(R, write, g_dev.num_sms, st);
         if (S.coef && c0 < S.coef_n && c0 + n >= S.coef_n) S.coef_valid = true;   // LOD0 transform kept
         if (prof) {
-            cudaEventRecord(S.c->ev[1], S.c->stream);
+            cudaEventRecord(S.c->ev[1], st);
             cudaEventSynchronize(S.c->ev[1]);
             // forward: volume bytes in (the lists it writes are scratch, not counted)
             if (from_cache)   // coefficients in, lists out (scratch, not counted)
@@ -113,6 +115,31 @@ static int run_range(EncState &S, uint64_t a0, uint64_t a1, bool write) {
                          0, n);
         }
     }
+    return 0;
+}
+
+// The same over [0, total): LOD0 on the context's stream and the coarser LODs
+// beside it on the second stream, with their own list scratch. The coarser LODs
+// are few atoms but the finest-quantised ones (q down to 0.05): one of them is a
+// serial coder chain longer than a whole LOD0 pass, so run after LOD0 it would
+// add its length. Serial under per-stage measurement (its events are per stream).
+static int run_split(EncState &S, uint64_t na0, uint64_t total, bool write) {
+    vcd_ctx *c = S.c;
+    cudaStream_t side = (total > na0 && na0 && !vcd_prof_on()) ? vcd_side_stream(c) : NULL;
+    void *pe = NULL, *pm = NULL;
+    const uint64_t n1 = total - na0 < kChunk ? total - na0 : kChunk;
+    if (side && (vcd_scratch(c, VCD_BUF_EENT2, n1 * VCD_MAX_ENTRIES * 4 + 16, &pe) != cudaSuccess ||
+                 vcd_scratch(c, VCD_BUF_EMETA2, n1 * 4 + 16, &pm) != cudaSuccess)) {
+        cudaGetLastError();
+        side = NULL;
+    }
+    if (!side) return run_range(S, 0, total, write, c->stream, S.ent, S.meta);
+    cudaEventRecord(c->chunk_ev[0], c->stream);   // the side stream starts after the work queued so far
+    cudaStreamWaitEvent(side, c->chunk_ev[0], 0);
+    run_range(S, na0, total, write, side, (uint32_t *)pe, (uint32_t *)pm);
+    run_range(S, 0, na0, write, c->stream, S.ent, S.meta);
+    cudaEventRecord(c->chunk_ev[1], side);
+    cudaStreamWaitEvent(c->stream, c->chunk_ev[1], 0);
     return 0;
 }
 
@@ -206,7 +233,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
         float q = f_of(mid);
         CK(cudaMemsetAsync(S.red, 0, 16, st), "totals reset");
         set_q(S, 0, q);
-        run_range(S, 0, na0, false);
+        run_range(S, 0, na0, false, st, S.ent, S.meta);
         unsigned long long h[2];
         CK(cudaMemcpyAsync(h, S.red, 16, cudaMemcpyDeviceToHost, st), "totals read");
         CK(cudaStreamSynchronize(st), "rate control pass");
@@ -237,12 +264,13 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
 
     // ---- sizes of every atom at its LOD's q (LODs 1.. together in one pass)
     for (int l = 0; l < nlod; ++l) set_q(S, l, qs[l]);
-    if (have_best) CK(cudaMemcpyAsync(S.len, S.best, na0 * 4, cudaMemcpyDeviceToDevice, st), "restore sizes");
-    else {
+    if (have_best) {
+        CK(cudaMemcpyAsync(S.len, S.best, na0 * 4, cudaMemcpyDeviceToDevice, st), "restore sizes");
+        run_range(S, na0, total_atoms, false, st, S.ent, S.meta);
+    } else {
         CK(cudaMemsetAsync(S.red, 0, 16, st), "totals reset");
-        run_range(S, 0, na0, false);
+        run_split(S, na0, total_atoms, false);
     }
-    run_range(S, na0, total_atoms, false);
 
     // ---- canonical placement: exclusive scan of consumed bytes
     const uint64_t head = 128 + 16 * info->l1_cap;
@@ -274,7 +302,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     S.arc = (uint8_t *)p;
     P.arc = S.arc;
     cudaMemsetAsync(S.arc, 0, total, st);
-    run_range(S, 0, total_atoms, true);
+    run_split(S, na0, total_atoms, true);
     if (prof) cudaEventRecord(c->ev[4], st);
     launch_slots(P, st);
     if (prof) {   // one 16-byte slot per atom
