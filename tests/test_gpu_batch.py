@@ -98,3 +98,28 @@ def test_every_launch_shape_matches_plain(vc, gpu, golden, shape):
         assert L.vcg_set_batch_shape(0, 0, 0) == 0
     assert L.vcg_set_batch_shape(2, 256, 0) == vc.VC_ERR_RANGE
     assert L.vcg_set_batch_shape(4, 512, 1) == vc.VC_ERR_RANGE
+
+
+@pytest.mark.parametrize("shape", [(16, 512, 0), (16, 256, 0), (16, 256, 1)])
+def test_many_boxes_over_one_atom(vc, gpu, golden, shape):
+    """More boxes over one atom than the butterfly transform stages per atom
+    (64 windows): the boxes beyond them take the per-row path. Half the windows
+    cover all 32 planes of the atom in z, half are cropped in z."""
+    L = vc.lib()
+    assert L.vcg_set_batch_shape(*shape) == 0
+    try:
+        a = vc.Archive(load_archive(golden["synth_prime_97x131x65_t20"]))
+        rng = np.random.default_rng(15)
+        reqs = []
+        for i in range(150):   # every box holds voxel (40, 40, 40): LOD0 atom (1, 1, 1) = [32, 64)^3
+            x0, y0 = int(rng.integers(0, 41)), int(rng.integers(0, 41))
+            x1, y1 = int(rng.integers(41, 98)), int(rng.integers(41, 132))
+            if i % 2:
+                z0, z1 = int(rng.integers(0, 33)), int(rng.integers(64, 66))
+            else:
+                z0, z1 = int(rng.integers(33, 41)), int(rng.integers(41, 64))
+            reqs.append((0, (x0, y0, z0, x1, y1, z1)))
+        check(vc, a, reqs, on_device=True)
+        check(vc, a, reqs, on_device=False)
+    finally:
+        assert L.vcg_set_batch_shape(0, 0, 0) == 0
