@@ -208,6 +208,9 @@ int vcg_synth_volume_device(uint32_t nx, uint32_t ny, uint32_t nz, uint64_t seed
 // thread's last call. With profiling enabled, per-stage device times, launch
 // counts, algorithmic bytes read / written and work units are accumulated per
 // kernel stage and read back (and optionally reset) with vcg_profile_read.
+// Enabling it changes two schedules so that each stage can be timed alone: a
+// batch of regions runs its two kernels without the CUDA graph, and an encode
+// runs the coarser LODs after LOD0 rather than beside it on a second stream.
 typedef struct {
     char name[32];
     double ms;
