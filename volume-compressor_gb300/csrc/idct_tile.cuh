@@ -122,6 +122,21 @@ __device__ __forceinline__ void store_col(uint8_t *obase, uint64_t ox, uint64_t 
     }
 }
 
+// The same for a window that holds all 32 planes of the atom (lz0 = 0, lz1 =
+// 32): one pointer step per plane, no per-plane test.
+__device__ __forceinline__ void store_col_full(uint8_t *obase, uint64_t ox, uint64_t oy, const Crop &k, int y,
+                                               int lane, const int32_t (&o)[32], int32_t dc) {
+    if ((uint32_t)lane < k.lx0 || (uint32_t)lane >= k.lx1 || (uint32_t)y < k.ly0 || (uint32_t)y >= k.ly1) return;
+    uint8_t *p = obase + (uint64_t)(y - k.ly0) * ox + (lane - k.lx0);
+    const uint64_t plane = ox * oy;
+#pragma unroll
+    for (int z = 0; z < 32; ++z) {
+        const int32_t x = (int32_t)((uint32_t)o[z] + (uint32_t)dc);
+        *p = (uint8_t)(x < 0 ? 0 : x > 255 ? 255 : x);
+        p += plane;
+    }
+}
+
 template <int NT>
 __device__ __forceinline__ void zero_window(uint8_t *obase, uint64_t ox, uint64_t oy, const Crop &k) {
     const uint32_t cw = k.lx1 - k.lx0, ch = k.ly1 - k.ly0, cd = k.lz1 - k.lz0;

@@ -160,10 +160,12 @@ __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
         }
         const int32_t dc = J.arc[e.off];
         idct_tile_xy<kIdctThreads>(T, J.arc, e, c, J.ent + J.ent_off[t], J.scan, J.band_start, dqs, dqb, alt);
+        const bool full = k.lz0 == 0 && k.lz1 == 32;
         for (int y = warp; y < 32; y += kIdctThreads / 32) {
             int32_t o[32];
             idct_col_z(T, y, lane, o);
-            store_col(obase, J.ox, J.oy, k, y, lane, o, dc);
+            if (full) store_col_full(obase, J.ox, J.oy, k, y, lane, o, dc);
+            else store_col(obase, J.ox, J.oy, k, y, lane, o, dc);
         }
         __syncthreads();
     }
