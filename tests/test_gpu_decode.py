@@ -227,3 +227,25 @@ def test_large_decode_into_pinned_memory_overlaps_copy_out(vc, gpu):
         assert s_ref == vc.VC_ERR_FORMAT
     finally:
         L.vcg_free_host(pinned)
+
+
+def test_large_decode_into_pageable_memory(vc, gpu):
+    """Outputs of >= 16 MiB in pageable memory are copied out through pinned
+    32 MiB bounce chunks by host threads: the bytes equal a decode into device
+    memory for whole chunks, a ragged last chunk and an output just below the
+    threshold (one plain copy)."""
+    n = 512
+    dv = vc.synth_device(n, n, n, vc.config_seed(2))
+    s, data = vc.encode_q(dv, 10.0, [2.0 * 0.6 ** l for l in range(8)], on_device=(n, n, n))
+    assert s == 0
+    dv.free()
+    a = vc.Archive(data)
+    for box in [(0, 0, 0, n, n, n), (3, 5, 7, 509, 487, 311), (0, 0, 0, 256, 256, 255)]:
+        nb = (box[3] - box[0]) * (box[4] - box[1]) * (box[5] - box[2])
+        host = np.full(nb, 0x77, np.uint8)
+        st, _ = a.decode_region(0, box, host)
+        assert st == vc.VC_OK
+        dbuf = vc.DeviceBuffer(nb)
+        assert a.decode_region_device(0, box, dbuf) == vc.VC_OK
+        assert np.array_equal(host, dbuf.download(nb)), box
+        dbuf.free()
