@@ -8,6 +8,7 @@
 // the first batch (all candidates produce identical bytes); threads that start
 // later take the tuned shape.
 #include <cuda_runtime.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -38,6 +39,53 @@ static size_t cap_of(const vcd_ctx *c, int slot) { return c->cap[slot]; }
 static int g_tuned_shape = 0;
 // shape set by vcg_set_batch_shape, same packing (0 = autotune)
 static int g_forced_shape = 0;
+
+// Staged outputs (request i at its 16-byte-aligned offset in src) to the callers'
+// buffers. From 16 MiB on, kCopyThreads threads each copy the parts of the
+// requests inside one contiguous stripe of src.
+namespace {
+constexpr int kCopyThreads = 12;
+constexpr uint64_t kCopyParallelMin = 16ull << 20;
+
+struct CopyJob {
+    const vcd_batch *b;
+    uint8_t *const *out;
+    const uint8_t *src;
+    uint64_t lo, hi;   // stripe of src
+};
+
+static void *copy_stripe(void *p) {
+    const CopyJob &j = *(const CopyJob *)p;
+    uint64_t o = 0;
+    for (uint32_t i = 0; i < j.b->n_req && o < j.hi; ++i) {
+        const vcd_boxreq &r = j.b->reqs[i];
+        const uint64_t n = (uint64_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
+        const uint64_t a = o > j.lo ? o : j.lo, e = o + n < j.hi ? o + n : j.hi;
+        if (j.out[i] && a < e) memcpy(j.out[i] + (a - o), j.src + a, e - a);
+        o += (n + 15) & ~15ull;
+    }
+    return NULL;
+}
+}  // namespace
+
+static void copy_to_requests(const vcd_batch *b, uint8_t *const *out, const uint8_t *src, uint64_t total) {
+    CopyJob jobs[kCopyThreads];
+    pthread_t th[kCopyThreads];
+    const int nt = total >= kCopyParallelMin ? kCopyThreads : 1;
+    const uint64_t per = (total + nt - 1) / nt;
+    int started = 0;
+    for (int t = 0; t < nt; ++t) {
+        jobs[t] = {b, out, src, (uint64_t)t * per, (uint64_t)(t + 1) * per < total ? (uint64_t)(t + 1) * per : total};
+        if (t == 0 || pthread_create(&th[t], NULL, copy_stripe, &jobs[t]) != 0) {
+            if (t) copy_stripe(&jobs[t]);   // no thread: this one copies the stripe itself
+        } else {
+            started |= 1 << t;
+        }
+    }
+    copy_stripe(&jobs[0]);
+    for (int t = 1; t < nt; ++t)
+        if (started & (1 << t)) pthread_join(th[t], NULL);
+}
 
 extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *const *host_out, uint32_t *req_err) {
     vcd_ctx *c = vcd_thread_ctx();
@@ -185,13 +233,7 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
         CKB(vcd_pinned(c, out_total + 16, &pin), "batch staging");
         CKB(cudaMemcpyAsync(pin, p_out, out_total, cudaMemcpyDeviceToHost, st), "batch copy-out");
         CKB(cudaStreamSynchronize(st), "batch copy-out");
-        uint64_t o = 0;
-        for (uint32_t i = 0; i < b->n_req; ++i) {
-            const vcd_boxreq &r = b->reqs[i];
-            const uint64_t n = (uint64_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
-            if (host_out[i]) memcpy(host_out[i], (uint8_t *)pin + o, n);
-            o += (n + 15) & ~15ull;
-        }
+        copy_to_requests(b, host_out, (const uint8_t *)pin, out_total);
     }
     return 0;
 }
