@@ -52,8 +52,11 @@ def test_server_mix_equals_alone(vc, gpu, golden, budget, max_batch, workers):
     outs, res, batches = run_mixed(vc, a, reqs, threads=4, budget=budget, max_batch=max_batch, workers=workers)
     check_alone(vc, a, reqs, outs, res)
     assert batches >= -(-len(reqs) // max_batch)
-    if budget == 1:   # every request exceeds the budget: each one runs alone
-        assert batches == len(reqs)
+    if budget == 1:
+        # every non-empty box exceeds the budget and runs alone; empty boxes hold
+        # no device memory, so two of them that meet in the queue may share a batch
+        n_boxes = sum(1 for _, b in reqs if box_bytes(b) > 0)
+        assert n_boxes <= batches <= len(reqs)
 
 
 @pytest.mark.gpu

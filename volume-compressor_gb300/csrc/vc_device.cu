@@ -74,6 +74,7 @@ static void ctx_free(void *p) {
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     if (c->copy_stream) {
         for (int i = 0; i < VCD_SLABS; ++i) cudaEventDestroy(c->chunk_ev[i]);
+        for (int i = 0; i < 4; ++i) cudaEventDestroy(c->ring_ev[i]);
         cudaStreamDestroy(c->copy_stream);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -250,6 +251,7 @@ cudaStream_t vcd_side_stream(vcd_ctx *c) {
             return NULL;
         }
         for (int i = 0; i < VCD_SLABS; ++i) cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming);
+        for (int i = 0; i < 4; ++i) cudaEventCreateWithFlags(&c->ring_ev[i], cudaEventDisableTiming);
     }
     return c->copy_stream;
 }
@@ -257,10 +259,12 @@ cudaStream_t vcd_side_stream(vcd_ctx *c) {
 // ---------------------------------------------------------------- pageable copy-out
 // Device -> pageable host memory for large outputs. A plain cudaMemcpy into
 // pageable memory is staged by the driver at about 20 GB/s on this machine; here the
-// device copies 32 MiB chunks into a ring of 4 pinned slots on the context's
-// stream while kBounceThreads host threads copy each finished chunk into the
-// destination (each thread a stripe of it). A slot is refilled once every
-// thread has finished the chunk in it.
+// device copies 32 MiB chunks into a ring of 4 pinned slots on stream cs while
+// kBounceThreads host threads copy each finished chunk into the destination
+// (each thread a stripe of it). A slot is refilled once every thread has
+// finished the chunk in it. With slabs, the copy of a chunk first waits for the
+// event of the slab whose end covers it, so the copy-out follows a transform
+// that is still running.
 namespace {
 constexpr size_t kBounceChunk = 32ull << 20;
 constexpr size_t kBounceMin = 16ull << 20;   // smaller outputs: one plain copy
@@ -269,6 +273,10 @@ constexpr int kBounceThreads = 12;   // 1 GiB LOD0 decode into pageable memory, 
 
 struct Bounce {
     vcd_ctx *c;
+    cudaStream_t cs;
+    const uint64_t *slab_end;    // optional: byte end of each slab of the source, ascending
+    const cudaEvent_t *slab_ev;  // and the event recorded when that slab is written
+    int nslab;
     uint8_t *dst;
     const uint8_t *src;
     uint8_t *ring;
@@ -288,9 +296,17 @@ static size_t chunk_len(const Bounce &b, uint32_t k) {
 
 static cudaError_t bounce_issue(Bounce &b, uint32_t k) {   // device chunk k into its slot (mu held)
     const int slot = (int)(k % kBounceRing);
-    cudaError_t e = cudaMemcpyAsync(b.ring + (size_t)slot * kBounceChunk, b.src + (size_t)k * kBounceChunk,
-                                    chunk_len(b, k), cudaMemcpyDeviceToHost, b.c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(b.c->chunk_ev[slot], b.c->stream);
+    cudaError_t e = cudaSuccess;
+    if (b.nslab) {   // the slab that completes this chunk
+        const uint64_t end = (uint64_t)k * kBounceChunk + chunk_len(b, k);
+        int j = 0;
+        while (j + 1 < b.nslab && b.slab_end[j] < end) ++j;
+        e = cudaStreamWaitEvent(b.cs, b.slab_ev[j], 0);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b.ring + (size_t)slot * kBounceChunk, b.src + (size_t)k * kBounceChunk, chunk_len(b, k),
+                            cudaMemcpyDeviceToHost, b.cs);
+    if (e == cudaSuccess) e = cudaEventRecord(b.c->ring_ev[slot], b.cs);
     b.done[slot] = 0;
     return e;
 }
@@ -311,7 +327,7 @@ static void *bounce_worker(void *p) {
         pthread_mutex_unlock(&b.mu);
         if (stop) break;
         const int slot = (int)(k % kBounceRing);
-        const cudaError_t e = cudaEventSynchronize(b.c->chunk_ev[slot]);
+        const cudaError_t e = cudaEventSynchronize(b.c->ring_ev[slot]);
         const size_t len = chunk_len(b, k), per = (len + kBounceThreads - 1) / kBounceThreads;
         const size_t lo = (size_t)w->id * per < len ? (size_t)w->id * per : len;
         const size_t hi = lo + per < len ? lo + per : len;
@@ -328,16 +344,20 @@ static void *bounce_worker(void *p) {
 }  // namespace
 
 // Returns cudaSuccess, or the first error (the destination is then incomplete).
-static cudaError_t copy_out_pageable(vcd_ctx *c, uint8_t *dst, const uint8_t *src_dev, size_t bytes) {
+// cs: the stream of the device copies; slab_end / slab_ev / nslab: see Bounce.
+static cudaError_t copy_out_pageable(vcd_ctx *c, uint8_t *dst, const uint8_t *src_dev, size_t bytes, cudaStream_t cs,
+                                     const uint64_t *slab_end, const cudaEvent_t *slab_ev, int nslab) {
     void *pin = NULL;
     cudaError_t e = vcd_pinned(c, kBounceChunk * kBounceRing, &pin);
     if (e != cudaSuccess || !vcd_side_stream(c)) {   // the slot events live with the second stream
+        if (e == cudaSuccess && nslab) e = cudaStreamSynchronize(c->stream);
         if (e == cudaSuccess) e = cudaMemcpy(dst, src_dev, bytes, cudaMemcpyDeviceToHost);
         return e;
     }
     Bounce b;
     memset(&b, 0, sizeof b);
-    b.c = c; b.dst = dst; b.src = src_dev; b.ring = (uint8_t *)pin; b.bytes = bytes;
+    b.c = c; b.cs = cs; b.slab_end = slab_end; b.slab_ev = slab_ev; b.nslab = nslab;
+    b.dst = dst; b.src = src_dev; b.ring = (uint8_t *)pin; b.bytes = bytes;
     b.n_chunks = (uint32_t)((bytes + kBounceChunk - 1) / kBounceChunk);
     b.err = cudaSuccess;
     pthread_mutex_init(&b.mu, NULL);
@@ -372,7 +392,7 @@ static cudaError_t copy_out_pageable(vcd_ctx *c, uint8_t *dst, const uint8_t *sr
     for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
     pthread_cond_destroy(&b.cv);
     pthread_mutex_destroy(&b.mu);
-    const cudaError_t se = cudaStreamSynchronize(c->stream);   // no copy into the ring still in flight
+    const cudaError_t se = cudaStreamSynchronize(cs);   // no copy into the ring still in flight
     if (b.err == cudaSuccess) b.err = se;
     return b.err;
 }
@@ -439,13 +459,16 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     // with a malformed atom is known before any byte reaches the caller.
     // (only when every atom of the box is decoded: a box cut short by a bad
     // payload range keeps the exact per-atom copy below)
-    bool piped = false;
+    // (pageable destinations take the same slabs, copied out through pinned
+    // bounce chunks by host threads)
+    bool piped = false, bounce = false;
     const uint64_t layer = (uint64_t)r->bnx * r->bny, layers = layer ? n / layer : 0;
     if (out_host && out_bytes >= (64ull << 20) && n == box_atoms && layers * layer == n && layers >= 2) {
         cudaPointerAttributes pa;
-        piped = cudaPointerGetAttributes(&pa, out_host) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        const bool pinned = cudaPointerGetAttributes(&pa, out_host) == cudaSuccess && pa.type == cudaMemoryTypeHost;
         cudaGetLastError();
-        if (piped && !vcd_side_stream(c)) piped = false;
+        piped = vcd_side_stream(c) != NULL;
+        bounce = piped && !pinned;
     }
     if (piped) {
         launch_decode_front(J, g_dev.num_sms, c->stream, &ev);
@@ -461,6 +484,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
         } else {
             const uint64_t plane = (uint64_t)J.ox * J.oy;
             const uint64_t per = (layers + VCD_SLABS - 1) / VCD_SLABS;
+            uint64_t slab_end[VCD_SLABS];
             int k = 0;
             for (uint64_t l0 = 0; l0 < layers; l0 += per, ++k) {
                 const uint64_t l1 = l0 + per < layers ? l0 + per : layers;
@@ -468,11 +492,20 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
                 cudaEventRecord(c->chunk_ev[k], c->stream);
                 const uint64_t zlo = (r->baz + l0) * 32 > r->z0 ? (r->baz + l0) * 32 : r->z0;
                 const uint64_t zhi = (r->baz + l1) * 32 < r->z1 ? (r->baz + l1) * 32 : r->z1;
-                cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0);
-                cudaMemcpyAsync(out_host + (zlo - r->z0) * plane, (uint8_t *)p_out + (zlo - r->z0) * plane,
-                                (zhi - zlo) * plane, cudaMemcpyDeviceToHost, c->copy_stream);
+                slab_end[k] = (zhi - r->z0) * plane;
+                if (!bounce) {
+                    cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0);
+                    cudaMemcpyAsync(out_host + (zlo - r->z0) * plane, (uint8_t *)p_out + (zlo - r->z0) * plane,
+                                    (zhi - zlo) * plane, cudaMemcpyDeviceToHost, c->copy_stream);
+                }
             }
             cudaEventRecord(ev.ev[3], c->stream);
+            if (bounce &&
+                (e = copy_out_pageable(c, out_host, (const uint8_t *)p_out, out_bytes, c->copy_stream, slab_end,
+                                       c->chunk_ev, k)) != cudaSuccess) {
+                vcd_set_error("decode copy-out", e);
+                return vcd_status_of(e);
+            }
         }
     } else {
         launch_decode_front(J, g_dev.num_sms, c->stream, &ev);
@@ -516,7 +549,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
                               (cudaPointerGetAttributes(&pa, out_host) != cudaSuccess || pa.type != cudaMemoryTypeHost);
         cudaGetLastError();
         if (pageable) {
-            e = copy_out_pageable(c, out_host, (const uint8_t *)p_out, out_bytes);
+            e = copy_out_pageable(c, out_host, (const uint8_t *)p_out, out_bytes, c->stream, NULL, NULL, 0);
         } else if ((e = cudaMemcpyAsync(out_host, p_out, out_bytes, cudaMemcpyDeviceToHost, c->stream)) == cudaSuccess) {
             e = cudaStreamSynchronize(c->stream);
         }

@@ -34,6 +34,7 @@ struct vcd_ctx {
     // with the inverse transform; the coarser LODs' coder passes beside LOD0's
     cudaStream_t copy_stream;
     cudaEvent_t chunk_ev[VCD_SLABS];
+    cudaEvent_t ring_ev[4];      // pinned bounce slots of a copy-out into pageable memory
     // streamed decode: pinned staging filled by the read callback, copied to VCD_BUF_STG
     uint8_t *stage_host;
     size_t stage_cap;
@@ -67,7 +68,7 @@ extern vcd_device g_dev;
 vcd_ctx *vcd_thread_ctx(void);
 cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out);
 cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out);
-// the context's second stream and its VCD_SLABS events, created on first use; NULL if that fails
+// the context's second stream with its slab and bounce-slot events, created on first use; NULL if that fails
 cudaStream_t vcd_side_stream(vcd_ctx *c);
 void vcd_set_error(const char *what, cudaError_t e);
 int vcd_status_of(cudaError_t e);
