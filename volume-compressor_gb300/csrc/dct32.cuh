@@ -17,6 +17,10 @@ namespace vcg {
 
 constexpr int kCm[32][32] = VC_CMAT_INIT;
 
+// The same in constant memory, for loops with a computed index (the int8 piece
+// tables, the first inverse pass of sparse atoms).
+static __constant__ int32_t c_cmat[32][32] = VC_CMAT_INIT;
+
 // CMATA[k][n]; with constant indices (fully unrolled loops) it folds to an immediate.
 __host__ __device__ constexpr int cmat(int k, int n) {
     constexpr int t[32][32] = VC_CMAT_INIT;

@@ -13,11 +13,10 @@
 #pragma once
 #include <stdint.h>
 
+#include "dct32.cuh"
 #include "vc_release_tables.h"
 
 namespace vcg {
-
-__constant__ int32_t c_cmat[32][32] = VC_CMAT_INIT;
 
 // Byte of element n in a 32-byte piece line, arranged so that lane (g, t) of
 // an m16n8k32 B fragment finds its elements n = 4t..4t+3 and 16+4t..16+4t+3 as
