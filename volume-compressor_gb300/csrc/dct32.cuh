@@ -17,8 +17,8 @@ namespace vcg {
 
 constexpr int kCm[32][32] = VC_CMAT_INIT;
 
-// The same in constant memory, for loops with a computed index (the int8 piece
-// tables, the first inverse pass of sparse atoms).
+// The same in constant memory, for loops with a computed index (the int8
+// tensor-core transform builds its matrix pieces from it).
 static __constant__ int32_t c_cmat[32][32] = VC_CMAT_INIT;
 
 // CMATA[k][n]; with constant indices (fully unrolled loops) it folds to an immediate.
