@@ -117,9 +117,12 @@ def test_oracle_lane_rule_matches_reference(oracle, nz):
         want = R.ds_downscale2x(vol, 1, a)
         assert np.array_equal(O.ds_downscale2x(vol, 1, a), want), ox
         O.lib().orc_ds_set_fused(0)
-        unf = np.array([[O.lib().orc_ds_cell(np.ascontiguousarray(
-            [vol[dz, 2 * y + dy, 2 * x + dx] for dz in (0, 1) for dy in (0, 1) for dx in (0, 1)], np.uint8).ctypes.data, 1, a)
-            for x in range(ox)] for y in range(3)])
+        unf = np.zeros((3, ox), np.int64)
+        for y in range(3):
+            for x in range(ox):
+                cell = np.ascontiguousarray(
+                    [vol[dz, 2 * y + dy, 2 * x + dx] for dz in (0, 1) for dy in (0, 1) for dx in (0, 1)], np.uint8)
+                unf[y, x] = O.lib().orc_ds_cell(cell.ctypes.data, 1, a)   # cell stays alive across the call
         O.lib().orc_ds_set_fused(1)
         unfused_seen += int((want[0] == unf).all(axis=0)[: ox & ~7].sum()) if nz == 2 else 0
     if nz == 2:

@@ -182,3 +182,37 @@ def test_oracle_encode_random_dims_matches_reference(oracle, ref):
         data_ref, q0 = ref.ref_encode(vol, t)
         s, data = oracle.encode(vol, t)
         assert s == 0 and data == data_ref, (nx, ny, nz, t)
+
+
+def test_forward_coefficients_fit_seventeen_bits(oracle):
+    """The GPU rate-control quantiser keeps each LOD0 coefficient packed with
+    its class and sign, the magnitude in 17 bits. The transform of 8-bit voxels
+    minus any centre in [0, 255] stays far below 2^17: the largest magnitude is
+    the DC coefficient of a block at 255 above or below its centre, 46,132 (the
+    DC row of the matrix has the largest absolute sum, 32 x 2896), and no
+    extreme pattern exceeds it."""
+    import ctypes
+    L = oracle.lib()
+    rng = np.random.default_rng(17)
+    x, y, z = np.meshgrid(np.arange(32), np.arange(32), np.arange(32), indexing="xy")
+    patterns = [np.full(32768, 255, np.uint8), np.zeros(32768, np.uint8),
+                (((x + y + z) & 1) * 255).astype(np.uint8).ravel(), ((x & 1) * 255).astype(np.uint8).ravel(),
+                ((((x >> 2) + (y >> 3) + z) & 1) * 255).astype(np.uint8).ravel()]
+    patterns += [(rng.integers(0, 2, 32768) * 255).astype(np.uint8) for _ in range(6)]
+    one = np.zeros(32768, np.uint8)
+    one[0] = 255
+    patterns.append(one)
+    peak = 0
+    coef = np.zeros(32768, np.int32)
+    for vox in patterns:
+        for dc in (0, 128, 255):
+            L.orc_fdct(vox.ctypes.data, ctypes.c_int32(dc), coef.ctypes.data)
+            peak = max(peak, int(np.abs(coef).max()))
+    dc_peak = 0
+    for v, c in ((255, 0), (0, 255)):   # 255 above and below the centre
+        block = np.full(32768, v, np.uint8)
+        L.orc_fdct(block.ctypes.data, ctypes.c_int32(c), coef.ctypes.data)
+        dc_peak = max(dc_peak, int(abs(coef[0])))
+    assert dc_peak == 46132
+    assert peak == dc_peak
+    assert peak < (1 << 17)
