@@ -49,9 +49,10 @@ __device__ __forceinline__ uint32_t quant_class(uint32_t r, const uint32_t *alt)
     return f + 94u * ((alt[r >> 5] >> (r & 31u)) & 1u);
 }
 
-// A coefficient with its class, as the quantiser needs it: |cf| (< 2^17: the
-// transform of 8-bit voxels stays below 46,300) in bits 0-16, the class in bits
-// 17-24, the sign in bit 31. Quantising it needs no scan order or class lookup.
+// A coefficient with its class, as the quantiser needs it: |cf| in bits 0-16
+// (the transform of 8-bit voxels about a centre in [0, 255] reaches at most
+// 46,132, the DC of a block 255 away from its centre), the class in bits 17-24,
+// the sign in bit 31. Quantising it needs no scan order or class lookup.
 __device__ __forceinline__ uint32_t coef_pack(int32_t cf, uint32_t r, const uint32_t *alt) {
     const uint32_t mag = cf < 0 ? 0u - (uint32_t)cf : (uint32_t)cf;
     return mag | (quant_class(r, alt) << 17) | (cf < 0 ? 0x80000000u : 0u);
