@@ -181,6 +181,14 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows), "source": "nvidia-smi, 200 ms"}
 
 
+# What bounds each decode stage, from the ncu captures of this workload (an HBM
+# fraction alone misreads a latency-bound kernel).
+LIMITER = {
+    "rc_decode": "dependency chain of each serial range decoder: 44 % issue active, DRAM under 1 % busy (ncu)",
+    "idct": "integer pipes of the inverse passes: 52 % issue active, DRAM 6 % busy (ncu)",
+}
+
+
 def dram_traffic(kernel, units):
     """DRAM bytes (read + write) of one launch of `kernel` processing `units`
     atoms, scaled from the per-atom figure of an ncu capture committed in
@@ -1128,7 +1136,8 @@ def gb300_arm(args, dist):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": dram_traffic(dom, st_["units"] / max(1, st_["launches"])),
                      "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
+                     "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
+                     "limiter": LIMITER.get(dom)},
         "stages": {k: {"ms_per_step": v["ms"] / args.steps, "GBps_algorithmic":
                        (v["bytes_read"] + v["bytes_written"]) / max(1e-9, v["ms"] / 1e3) / 1e9}
                    for k, v in stats.items()},
