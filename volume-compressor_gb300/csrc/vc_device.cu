@@ -258,7 +258,8 @@ cudaStream_t vcd_side_stream(vcd_ctx *c) {
 
 // ---------------------------------------------------------------- pageable copy-out
 // Device -> pageable host memory for large outputs. A plain cudaMemcpy into
-// pageable memory is staged by the driver at about 20 GB/s on this machine; here the
+// pageable memory goes through the CUDA runtime's own staging at about 20 GB/s
+// (measured on a GB300 with a Grace host); here the
 // device copies 32 MiB chunks into a ring of 4 pinned slots on stream cs while
 // kBounceThreads host threads copy each finished chunk into the destination
 // (each thread a stripe of it). A slot is refilled once every thread has
