@@ -58,8 +58,7 @@ extern "C" int vcd_repack(vcd_archive *d, const uint8_t *head, uint64_t head_len
                                                                       (uint8_t *)p_out);
     }
     cudaEventRecord(c->ev[1], st);
-    if ((e = cudaMemcpyAsync(host_out, p_out, total_len, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) {
+    if ((e = vcd_copy_to_host(c, host_out, p_out, total_len)) != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) {
         vcd_set_error("repack", e);
         return vcd_status_of(e);
     }

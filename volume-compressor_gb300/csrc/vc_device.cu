@@ -398,6 +398,134 @@ static cudaError_t copy_out_pageable(vcd_ctx *c, uint8_t *dst, const uint8_t *sr
     return b.err;
 }
 
+// Pageable host -> device for large inputs, the same ring the other way: the
+// kBounceThreads threads copy each 32 MiB chunk of the source into a pinned
+// slot (each a stripe of it), then the chunk is copied to the device on the
+// context's stream; a slot is refilled once its previous copy to the device has
+// completed.
+namespace {
+struct BounceIn {
+    vcd_ctx *c;
+    uint8_t *dst;
+    const uint8_t *src;
+    uint8_t *ring;
+    size_t bytes;
+    uint32_t n_chunks;
+    pthread_mutex_t mu;
+    pthread_cond_t cv;
+    uint32_t issued;               // chunks whose device copy has been queued
+    uint32_t filled[kBounceRing];  // threads done filling the chunk in each slot
+    cudaError_t err;
+};
+
+static size_t in_len(const BounceIn &b, uint32_t k) {
+    const size_t off = (size_t)k * kBounceChunk;
+    return b.bytes - off < kBounceChunk ? b.bytes - off : kBounceChunk;
+}
+
+struct BounceInWorker {
+    BounceIn *b;
+    int id;
+};
+
+static void *bounce_in_worker(void *p) {
+    BounceInWorker *w = (BounceInWorker *)p;
+    BounceIn &b = *w->b;
+    cudaSetDevice(g_dev.device);
+    for (uint32_t k = 0; k < b.n_chunks; ++k) {
+        const int slot = (int)(k % kBounceRing);
+        if (k >= (uint32_t)kBounceRing) {   // the slot's previous chunk must have reached the device
+            pthread_mutex_lock(&b.mu);
+            while (b.issued <= k - kBounceRing && b.err == cudaSuccess) pthread_cond_wait(&b.cv, &b.mu);
+            const bool stop = b.err != cudaSuccess;
+            pthread_mutex_unlock(&b.mu);
+            if (stop) break;
+            const cudaError_t e = cudaEventSynchronize(b.c->ring_ev[slot]);
+            if (e != cudaSuccess) {
+                pthread_mutex_lock(&b.mu);
+                if (b.err == cudaSuccess) b.err = e;
+                pthread_cond_broadcast(&b.cv);
+                pthread_mutex_unlock(&b.mu);
+                break;
+            }
+        }
+        const size_t len = in_len(b, k), per = (len + kBounceThreads - 1) / kBounceThreads;
+        const size_t lo = (size_t)w->id * per < len ? (size_t)w->id * per : len;
+        const size_t hi = lo + per < len ? lo + per : len;
+        if (hi > lo) memcpy(b.ring + (size_t)slot * kBounceChunk + lo, b.src + (size_t)k * kBounceChunk + lo, hi - lo);
+        pthread_mutex_lock(&b.mu);
+        ++b.filled[slot];
+        pthread_cond_broadcast(&b.cv);
+        pthread_mutex_unlock(&b.mu);
+    }
+    return NULL;
+}
+}  // namespace
+
+static cudaError_t copy_in_pageable(vcd_ctx *c, uint8_t *dst_dev, const uint8_t *src, size_t bytes) {
+    void *pin = NULL;
+    cudaError_t e = vcd_pinned(c, kBounceChunk * kBounceRing, &pin);
+    if (e != cudaSuccess || !vcd_side_stream(c))   // the slot events live with the second stream
+        return e != cudaSuccess ? e : cudaMemcpy(dst_dev, src, bytes, cudaMemcpyHostToDevice);
+    BounceIn b;
+    memset(&b, 0, sizeof b);
+    b.c = c; b.dst = dst_dev; b.src = src; b.ring = (uint8_t *)pin; b.bytes = bytes;
+    b.n_chunks = (uint32_t)((bytes + kBounceChunk - 1) / kBounceChunk);
+    b.err = cudaSuccess;
+    pthread_mutex_init(&b.mu, NULL);
+    pthread_cond_init(&b.cv, NULL);
+    pthread_t th[kBounceThreads];
+    BounceInWorker wk[kBounceThreads];
+    int started = 0;
+    for (; started < kBounceThreads; ++started) {
+        wk[started].b = &b;
+        wk[started].id = started;
+        if (pthread_create(&th[started], NULL, bounce_in_worker, &wk[started]) != 0) break;
+    }
+    pthread_mutex_lock(&b.mu);
+    if (started < kBounceThreads) b.err = cudaErrorLaunchOutOfResources;
+    for (uint32_t k = 0; k < b.n_chunks && b.err == cudaSuccess; ++k) {
+        const int slot = (int)(k % kBounceRing);
+        while (b.filled[slot] < (uint32_t)kBounceThreads && b.err == cudaSuccess) pthread_cond_wait(&b.cv, &b.mu);
+        if (b.err != cudaSuccess) break;
+        cudaError_t ie = cudaMemcpyAsync(b.dst + (size_t)k * kBounceChunk, b.ring + (size_t)slot * kBounceChunk,
+                                         in_len(b, k), cudaMemcpyHostToDevice, c->stream);
+        if (ie == cudaSuccess) ie = cudaEventRecord(c->ring_ev[slot], c->stream);
+        b.filled[slot] = 0;
+        b.issued = k + 1;
+        if (ie != cudaSuccess) b.err = ie;
+        pthread_cond_broadcast(&b.cv);
+    }
+    pthread_cond_broadcast(&b.cv);
+    pthread_mutex_unlock(&b.mu);
+    for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
+    pthread_cond_destroy(&b.cv);
+    pthread_mutex_destroy(&b.mu);
+    const cudaError_t se = cudaStreamSynchronize(c->stream);   // the ring is free again
+    return b.err != cudaSuccess ? b.err : se;
+}
+
+static bool host_pageable(const void *p, size_t bytes) {
+    if (bytes < kBounceMin) return false;
+    cudaPointerAttributes pa;
+    const bool pinned = cudaPointerGetAttributes(&pa, p) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    return !pinned;
+}
+
+cudaError_t vcd_copy_to_host(vcd_ctx *c, void *dst, const void *src_dev, size_t bytes) {
+    if (host_pageable(dst, bytes))
+        return copy_out_pageable(c, (uint8_t *)dst, (const uint8_t *)src_dev, bytes, c->stream, NULL, NULL, 0);
+    cudaError_t e = cudaMemcpyAsync(dst, src_dev, bytes, cudaMemcpyDeviceToHost, c->stream);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+}
+
+cudaError_t vcd_copy_from_host(vcd_ctx *c, void *dst_dev, const void *src, size_t bytes) {
+    if (host_pageable(src, bytes)) return copy_in_pageable(c, (uint8_t *)dst_dev, (const uint8_t *)src, bytes);
+    cudaError_t e = cudaMemcpyAsync(dst_dev, src, bytes, cudaMemcpyHostToDevice, c->stream);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+}
+
 // ---------------------------------------------------------------- decode
 // One box decode from device bytes `arc` and atom table `atoms` (LOD raster, or
 // box order when box_table). last_ms spans from `t0` (or the first stage event).

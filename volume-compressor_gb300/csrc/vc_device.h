@@ -70,5 +70,10 @@ cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out);
 cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out);
 // the context's second stream with its slab and bounce-slot events, created on first use; NULL if that fails
 cudaStream_t vcd_side_stream(vcd_ctx *c);
+// Synchronous copies between device memory and host memory of any kind on the
+// context's stream (queued work first): pageable buffers of 16 MiB or more go
+// through pinned 32 MiB chunks copied by host threads, others in one copy.
+cudaError_t vcd_copy_to_host(vcd_ctx *c, void *dst, const void *src_dev, size_t bytes);
+cudaError_t vcd_copy_from_host(vcd_ctx *c, void *dst_dev, const void *src, size_t bytes);
 void vcd_set_error(const char *what, cudaError_t e);
 int vcd_status_of(cudaError_t e);

@@ -172,7 +172,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
         S.lvol[0] = vol;
     } else {
         CK(vcd_scratch(c, VCD_BUF_VOL, nvox[0], &p), "encode volume");
-        CK(cudaMemcpyAsync(p, vol, nvox[0], cudaMemcpyHostToDevice, st), "volume upload");
+        CK(vcd_copy_from_host(c, p, vol, nvox[0]), "volume upload");
         S.lvol[0] = (const uint8_t *)p;
     }
     CK(vcd_scratch(c, VCD_BUF_PYR, pyr_bytes + 16, &p), "pyramid");
@@ -345,8 +345,7 @@ extern "C" int vcd_encode(const uint8_t *vol, int on_dev, vcd_encode_info *info,
     e = cudaMemcpyAsync(S.arc, hd, head, cudaMemcpyHostToDevice, st);
     uint8_t *res = (uint8_t *)malloc(total);
     if (!res) { cudaStreamSynchronize(st); free(hd); return 3; }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(res, S.arc, total, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = vcd_copy_to_host(c, res, S.arc, total);   // after the head on the same stream
     if (e == cudaSuccess) e = cudaGetLastError();
     free(hd);
     if (e != cudaSuccess) { free(res); vcd_set_error("archive assembly", e); return vcd_status_of(e); }
