@@ -404,8 +404,7 @@ extern "C" int vcd_encode_segments(const vcd_seg *segs, int nseg, const float *q
         if (!na) continue;
         if ((e = vcd_scratch(c, VCD_BUF_VOL, (size_t)S.nx * S.ny * S.nz + 16, &p)) != cudaSuccess) break;
         const uint8_t *dvol = (const uint8_t *)p;
-        if ((e = cudaMemcpyAsync(p, S.vox, (size_t)S.nx * S.ny * S.nz, cudaMemcpyHostToDevice, st)) != cudaSuccess)
-            break;
+        if ((e = vcd_copy_from_host(c, p, S.vox, (size_t)S.nx * S.ny * S.nz)) != cudaSuccess) break;
         Layout lay;
         memset(&lay, 0, sizeof lay);
         lay.nlod = 1;
