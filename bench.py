@@ -51,6 +51,8 @@ def args_parse():
     p.add_argument("--no-sweep", action="store_true", help="skip the config-2 target / LOD sweep")
     p.add_argument("--dct-size", type=int, default=1024, help="edge of the DCT-forms volume")
     p.add_argument("--dct-reps", type=int, default=3, help="timed calls per DCT form and direction (0: one call)")
+    p.add_argument("--detail", default=os.path.join(ROOT, "gpurun_out", "bench_detail.json"),
+                   help="file that receives the full record (sweeps, batched, served, DCT, writer); '' for none")
     return p.parse_args()
 
 
@@ -962,7 +964,7 @@ def reference_arm(args, dist):
                                   "sample": f"full LOD0 decode ({nbytes} voxels) per step, parallel-for over atoms"},
                                  **host_info()),
             "e2e": {"value": gbps, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(_round(line), separators=(",", ":")), flush=True)
 
 
 def gb300_arm(args, dist):
@@ -1120,49 +1122,76 @@ def gb300_arm(args, dist):
             served = config5_served()
     if dist.rank != 0:
         return
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": dram_traffic(dom, st_["units"] / max(1, st_["launches"])),
+            "peak_source": peak_kind}
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "i32", "data": "synthetic",
         "config": {"workload": f"LOD0 decode, {n}^3 u8 synthetic scroll volume (seed 0x5EED0002), "
                                f"target_ratio {args.target:g}, archive resident in HBM",
-                   "volume": list(dims), "target_ratio": args.target, "q0": q0, "archive_bytes": len(data),
                    "l2": "flushed between timed steps (512 MiB device write)", "parallelism": f"replicas{dist.world}"},
-        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": nbytes,
-                "step_ms": [round(t * 1e3, 3) for t in e2e_t]},
-        "e2e_pageable": {"value": e2e_pg, "unit": "GB/s", "step_ms": [round(t * 1e3, 3) for t in pg_t],
-                         "note": "same calls, output in pageable memory (copied out through pinned bounce chunks)"},
+        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches,
-        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": dram_traffic(dom, st_["units"] / max(1, st_["launches"])),
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
-                     "limiter": LIMITER.get(dom)},
-        "stages": {k: {"ms_per_step": v["ms"] / args.steps, "GBps_algorithmic":
-                       (v["bytes_read"] + v["bytes_written"]) / max(1e-9, v["ms"] / 1e3) / 1e9}
-                   for k, v in stats.items()},
-        "encode_GBps": nbytes / (statistics.median(enc_ms) / 1e3) / 1e9,
-        "encode_with_rate_control_GBps": nbytes / (enc_full_ms / 1e3) / 1e9,
+        "roofline": roof,
+        "clocks": {k: clk.get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+        "bit_exact": {"archive_vs_reference": bit_exact_archive, "lod0_vs_reference": lod0_ok},
         "region_p50_us": lat[len(lat) // 2] if lat else None,
         "region_p99_us": lat[min(len(lat) - 1, int(len(lat) * 0.99))] if lat else None,
-        "bit_exact": {"archive_vs_reference": bit_exact_archive, "lod0_vs_reference": lod0_ok},
-        "clocks": clk,
     }
     if cpu:
-        line["cpu_baseline"] = cpu
-    if batched:
-        line["batched_regions"] = batched
-    if served:
-        line["served_regions"] = served
-    if dct:
-        line["dct_forms"] = dct
-    if sweep:
-        line["config2_sweep"] = sweep
-    if ds:
-        line["exporter_downscale"] = ds
-    if writer:
-        line["writer_append"] = writer
-    print(json.dumps(line), flush=True)
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    # everything else goes to the side file and to one earlier stdout line
+    detail = dict(line)
+    detail["config"] = dict(line["config"], volume=list(dims), target_ratio=args.target, q0=q0,
+                            archive_bytes=len(data))
+    detail["e2e"] = dict(line["e2e"], step_ms=[round(t * 1e3, 3) for t in e2e_t])
+    detail["e2e_pageable"] = {"value": e2e_pg, "unit": "GB/s", "step_ms": [round(t * 1e3, 3) for t in pg_t],
+                              "note": "same calls, output in pageable memory (copied out through pinned bounce chunks)"}
+    detail["roofline"] = dict(roof, algorithmic_bytes_per_launch=per_launch_bytes, ms_per_launch=per_launch_ms,
+                              limiter=LIMITER.get(dom))
+    detail["clocks"] = clk
+    detail["stages"] = {k: {"ms_per_step": v["ms"] / args.steps, "GBps_algorithmic":
+                            (v["bytes_read"] + v["bytes_written"]) / max(1e-9, v["ms"] / 1e3) / 1e9}
+                        for k, v in stats.items()}
+    detail["encode_GBps"] = nbytes / (statistics.median(enc_ms) / 1e3) / 1e9
+    detail["encode_with_rate_control_GBps"] = nbytes / (enc_full_ms / 1e3) / 1e9
+    if cpu:
+        detail["cpu_baseline"] = cpu
+    for key, val in (("batched_regions", batched), ("served_regions", served), ("dct_forms", dct),
+                     ("config2_sweep", sweep), ("exporter_downscale", ds), ("writer_append", writer)):
+        if val:
+            detail[key] = val
+    emit(line, detail, args.detail)
+
+
+def _round(v):
+    if isinstance(v, float):
+        return float(f"{v:.5g}")
+    if isinstance(v, dict):
+        return {k: _round(x) for k, x in v.items()}
+    if isinstance(v, list):
+        return [_round(x) for x in v]
+    return v
+
+
+def emit(line, detail, path):
+    """Writes the full record to `path` and as one stdout line tagged
+    "detail", then prints the headline as the LAST stdout line, compact (floats
+    to 5 significant digits), so that a reader that keeps only the tail of the
+    output still gets the whole headline object."""
+    if path:
+        try:
+            os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+            with open(path, "w") as f:
+                json.dump(detail, f, indent=1)
+        except OSError as e:
+            print(f"bench: cannot write {path}: {e}", file=sys.stderr)
+    print(json.dumps({"detail": detail}), flush=True)
+    sys.stderr.flush()
+    out = json.dumps(_round(line), separators=(",", ":"))
+    print(out, flush=True)
 
 
 def main():

@@ -233,6 +233,7 @@ int   vcg_copy(void *dst, const void *src, size_t bytes);
 int   vcg_memset(void *dst, int v, size_t bytes);
 int   vcg_sync(void);
 int   vcg_device_info(int *num_sms, int *cc_major, int *cc_minor);
+int   vcg_device_memory(size_t *free_bytes, size_t *total_bytes);   // cudaMemGetInfo of the library's device
 const char *vcg_last_error(void);
 
 #ifdef __cplusplus

@@ -6,6 +6,7 @@ regular vc_decode_atom output exactly, on two calls in a row (the calls share
 one fixed scratch array, so the second must not see the first's leftovers).
 
 This file is named to be collected last."""
+import ctypes
 import struct
 
 import numpy as np
@@ -62,3 +63,140 @@ def test_noalloc_rejects_more_than_its_limit(vc, gpu):
     lens[0] = 8
     assert L.vcg_decode_atoms_noalloc(buf.ptr, 1 << 16, vc.ptr(offs), vc.ptr(lens), 1, 1.0, buf.ptr) == \
         vc.VC_ERR_FORMAT
+
+
+class _RangeEncoder:
+    """Binary range encoder with the codec's arithmetic (12-bit probabilities of
+    a zero bit, shift-5 adaptation, bypass bits halve the range, five flush
+    shifts; src/vc/vc.c:344-401). Used only to craft a payload that no
+    encoder of the codec would write."""
+
+    def __init__(self):
+        self.low, self.range, self.cache, self.pending, self.out = 0, 0xFFFFFFFF, 0, 1, bytearray()
+
+    def _shift(self):
+        if (self.low & 0xFFFFFFFF) < 0xFF000000 or (self.low >> 32):
+            carry, b = self.low >> 32, self.cache
+            while True:
+                self.out.append((b + carry) & 0xFF)
+                b = 0xFF
+                self.pending -= 1
+                if not self.pending:
+                    break
+            self.cache = (self.low >> 24) & 0xFF
+        self.pending += 1
+        self.low = (self.low & 0x00FFFFFF) << 8
+
+    def _norm(self):
+        while self.range < (1 << 24):
+            self._shift()
+            self.range = (self.range << 8) & 0xFFFFFFFF
+
+    def bit(self, ctx, i, b):
+        r0 = (self.range * ctx[i]) >> 12
+        if b:
+            self.low += r0
+            self.range -= r0
+            ctx[i] -= ctx[i] >> 5
+        else:
+            self.range = r0
+            ctx[i] += (4096 - ctx[i]) >> 5
+        self._norm()
+
+    def bypass(self, b):
+        self.range >>= 1
+        if b:
+            self.low += self.range
+        self._norm()
+
+    def finish(self):
+        for _ in range(5):
+            self._shift()
+        return bytes(self.out)
+
+
+def _hostile_payload(dc=100, prefix_ones=40):
+    """[dc][coder bytes] of a stream whose first coefficient escapes with an
+    exponential-Golomb prefix of `prefix_ones` ones: longer than any level can
+    need, so a decoder must reject it as malformed."""
+    e = _RangeEncoder()
+    sig, mag = [2048] * 8, [2048] * 12
+    for i in range(15, -1, -1):   # EOB = 1
+        e.bypass((1 >> i) & 1)
+    e.bit(sig, 0, 1)              # scan position 0 (band 0) is significant
+    for k in range(12):           # unary magnitude saturates, then the escape
+        e.bit(mag, k, 1)
+    for _ in range(prefix_ones):
+        e.bypass(1)
+    return bytes([dc]) + e.finish()
+
+
+def _payloads(a, data, lod, atoms):
+    offs = np.zeros(len(atoms), np.uint64)
+    lens = np.zeros(len(atoms), np.uint32)
+    for i, (az, ay, ax) in enumerate(atoms):
+        cov, o, n = a.payload_range(lod, az, ay, ax)
+        offs[i], lens[i] = o, n
+    return offs, lens
+
+
+def test_noalloc_rejects_a_malformed_payload_then_decodes_correctly(vc, oracle, gpu, golden):
+    """A payload inside the buffer whose coder stream is malformed gives
+    VC_ERR_FORMAT (the oracle rejects it too); the scratch it leaves behind must
+    not change the next, correct call, which still equals vc_decode_atom."""
+    data = load_archive(golden["synth_prime_97x131x65_t20"])
+    bad = _hostile_payload()
+    out = np.zeros(32768, np.uint8)
+    assert oracle.lib().orc_decode_atom_payload(bad, len(bad), ctypes.c_float(1.0), vc.ptr(out)) == 1
+    a = vc.Archive(data)
+    base_q = struct.unpack_from("<8f", data, 72)
+    pad = (-len(data)) % 4
+    buf = np.frombuffer(data + bytes(pad) + bad, np.uint8)
+    dev = vc.DeviceBuffer(len(buf))
+    dev.upload(buf)
+    L = vc.lib()
+    atoms = _atoms(a, 0, 8)
+    offs, lens = _payloads(a, data, 0, atoms)
+    res = vc.DeviceBuffer(len(atoms) * 32768)
+    offs_bad, lens_bad = offs.copy(), lens.copy()
+    offs_bad[3], lens_bad[3] = len(data) + pad, len(bad)
+    s = L.vcg_decode_atoms_noalloc(dev.ptr, len(buf), vc.ptr(offs_bad), vc.ptr(lens_bad), len(atoms),
+                                   base_q[0], res.ptr)
+    assert s == vc.VC_ERR_FORMAT
+    assert vc.last_error()
+    s = L.vcg_decode_atoms_noalloc(dev.ptr, len(buf), vc.ptr(offs), vc.ptr(lens), len(atoms), base_q[0], res.ptr)
+    assert s == vc.VC_OK, vc.last_error()
+    got = res.download().reshape(len(atoms), 32768)
+    for i, (az, ay, ax) in enumerate(atoms):
+        s, ref = a.decode_atom(0, ax, ay, az)
+        assert s == vc.VC_OK and np.array_equal(got[i], ref), (az, ay, ax)
+
+
+def test_noalloc_allocates_no_device_memory(vc, gpu, golden):
+    """After the first call on the device (which sets up the scratch array),
+    repeated calls leave the device's free memory exactly where it was."""
+    data = load_archive(golden["synth_prime_97x131x65_t20"])
+    a = vc.Archive(data)
+    dev = vc.DeviceBuffer(len(data))
+    dev.upload(np.frombuffer(data, np.uint8))
+    base_q = struct.unpack_from("<8f", data, 72)
+    L = vc.lib()
+    calls = []
+    for lod in (0, 1, 0, 2):
+        atoms = _atoms(a, lod, 64)
+        offs, lens = _payloads(a, data, lod, atoms)
+        calls.append((lod, offs, lens, len(atoms)))
+    out = vc.DeviceBuffer(64 * 32768)
+    lod, offs, lens, n = calls[0]
+    assert L.vcg_decode_atoms_noalloc(dev.ptr, len(data), vc.ptr(offs), vc.ptr(lens), n, base_q[lod], out.ptr) == 0
+    assert vc.sync() == 0
+    s, free0, _ = vc.device_memory()
+    assert s == 0
+    for _ in range(3):
+        for lod, offs, lens, n in calls:
+            s = L.vcg_decode_atoms_noalloc(dev.ptr, len(data), vc.ptr(offs), vc.ptr(lens), n, base_q[lod], out.ptr)
+            assert s == vc.VC_OK, vc.last_error()
+    assert vc.sync() == 0
+    s, free1, _ = vc.device_memory()
+    assert s == 0
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"

@@ -307,11 +307,7 @@ static void launch_rc(const BatchJob &J, int num_sms, uint32_t max_ua, cudaStrea
 
 template <int NT>
 static void launch_tx(const BatchJob &J, int num_sms, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_idct_batch<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
-        attr = true;
-    }
+    smem_attr((const void *)k_idct_batch<NT>, (int)kTileSmem);
     k_idct_batch<NT><<<num_sms, NT, kTileSmem, s>>>(J);
 }
 
@@ -323,11 +319,7 @@ void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint3
     launch_rc(Jr, num_sms, max_ua, s);
     if (mid) cudaEventRecord(mid, s);
     if (shape.imma) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_idct_batch_imma<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kImmaSmem);
-            attr = true;
-        }
+        smem_attr((const void *)k_idct_batch_imma<256>, (int)kImmaSmem);
         k_idct_batch_imma<256><<<num_sms, 256, kImmaSmem, s>>>(J);
     } else if (shape.idct_threads == 512) {
         launch_tx<512>(J, num_sms, s);

@@ -33,6 +33,7 @@
 #include "../../include/vcg.h"
 #include "dct32.cuh"
 #include "imma.cuh"
+#include "kernels.cuh"
 #include "vc_device.h"
 
 namespace vcg {
@@ -315,26 +316,18 @@ static vc_status dct_run(const void *in, void *out, uint8_t *dc, vc_dims dims, i
     cudaEventRecord(c->ev[0], st);
     const char *name;
     if (form == VCG_DCT_BUTTERFLY) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_dct_bf<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileBytes);
-            cudaFuncSetAttribute(k_dct_bf<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileBytes);
-            attr = true;
-        }
+        smem_attr((const void *)k_dct_bf<false>, (int)kTileBytes);
+        smem_attr((const void *)k_dct_bf<true>, (int)kTileBytes);
         if (inverse) k_dct_bf<true><<<grid, kDctThreads, kTileBytes, st>>>(J);
         else k_dct_bf<false><<<grid, kDctThreads, kTileBytes, st>>>(J);
         name = inverse ? "dct_inverse_butterfly" : "dct_forward_butterfly";
     } else {
-        static bool attr = false;
         // piece planes; an atom redone with the butterfly reuses them as its tile
         const size_t planes_fwd = 2 * 2 * 32768, planes_inv = 2 * 3 * 32768;
         const size_t fwd_smem = planes_fwd > kTileBytes ? planes_fwd : kTileBytes;
         const size_t inv_smem = planes_inv > kTileBytes ? planes_inv : kTileBytes;
-        if (!attr) {
-            cudaFuncSetAttribute(k_dct_imma<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem);
-            cudaFuncSetAttribute(k_dct_imma<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)inv_smem);
-            attr = true;
-        }
+        smem_attr((const void *)k_dct_imma<false, 2>, (int)fwd_smem);
+        smem_attr((const void *)k_dct_imma<true, 3>, (int)inv_smem);
         if (inverse) k_dct_imma<true, 3><<<grid, kDctThreads, inv_smem, st>>>(J);
         else k_dct_imma<false, 2><<<grid, kDctThreads, fwd_smem, st>>>(J);
         name = inverse ? "dct_inverse_imma" : "dct_forward_imma";
@@ -357,10 +350,12 @@ static vc_status dct_run(const void *in, void *out, uint8_t *dc, vc_dims dims, i
 
 VC_API vc_status vcg_dct_forward(const uint8_t *vol_dev, vc_dims dims, int centre, int form, int32_t *coef_dev,
                                  uint8_t *dc_dev, uint32_t *redone) {
+    VCD_SCOPE();
     return dct_run(vol_dev, coef_dev, dc_dev, dims, centre, form, 0, redone);
 }
 
 VC_API vc_status vcg_dct_inverse(const int32_t *coef_dev, const uint8_t *dc_dev, vc_dims dims, int centre, int form,
                                  uint8_t *vol_dev, uint32_t *redone) {
+    VCD_SCOPE();
     return dct_run(coef_dev, vol_dev, const_cast<uint8_t *>(dc_dev), dims, centre, form, 1, redone);
 }

@@ -175,17 +175,9 @@ void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cu
     k_scan_u64<<<1, 1024, 0, s>>>(v, n, base, total);
 }
 
-static void idct_attr() {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_idct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIdctSmem);
-        attr = true;
-    }
-}
-
 void launch_idct(const DecodeJob &J, int num_sms, cudaStream_t s, uint64_t t_lo, uint64_t t_hi) {
-    idct_attr();
     if (t_hi <= t_lo) return;
+    smem_attr((const void *)k_idct, (int)kIdctSmem);
     DecodeJob Jr = J;
     Jr.t_lo = t_lo;
     Jr.t_hi = t_hi;

@@ -17,6 +17,7 @@
 
 #include "dct32.cuh"
 #include "k_encode.cuh"
+#include "kernels.cuh"
 #include "rangecoder.cuh"
 
 namespace vcg {
@@ -376,12 +377,8 @@ __global__ void k_gather_dc(const uint32_t *meta, uint64_t n, uint8_t *dc) {
 }
 
 void enc_set_smem() {
-    static bool done = false;
-    if (!done) {
-        cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-        cudaFuncSetAttribute(k_quant_cached, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQuantSmem);
-        done = true;
-    }
+    smem_attr((const void *)k_fwd, (int)kFwdSmem);
+    smem_attr((const void *)k_quant_cached, (int)kQuantSmem);
 }
 
 void launch_quant_cached(const FwdJob &J, int num_sms, cudaStream_t s) {

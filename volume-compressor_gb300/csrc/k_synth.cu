@@ -101,6 +101,7 @@ __global__ void k_syn_merge(const uint8_t *mask, uint64_t n, uint8_t *out) {
 
 // Generate the whole volume described by *cfg_host into device memory out_dev.
 VC_API int vcg_synth_device(const syn_cfg *cfg_host, uint8_t *out_dev) {
+    VCD_SCOPE();
     if (vcd_init() != 0) return 4;
     vcd_ctx *cx = vcd_thread_ctx();
     if (!cx) return 4;
@@ -143,36 +144,44 @@ VC_API int vcg_synth_device(const syn_cfg *cfg_host, uint8_t *out_dev) {
 
 // ---------------------------------------------------------------- device memory helpers
 VC_API void *vcg_alloc(size_t bytes) {
+    VCD_SCOPE();
     if (vcd_init() != 0) return NULL;
     void *p = NULL;
     return cudaMalloc(&p, bytes ? bytes : 1) == cudaSuccess ? p : NULL;
 }
 VC_API void vcg_free(void *p) {
+    VCD_SCOPE();
     if (p) cudaFree(p);
 }
 VC_API void *vcg_alloc_host(size_t bytes) {
+    VCD_SCOPE();
     if (vcd_init() != 0) return NULL;
     void *p = NULL;
     return cudaMallocHost(&p, bytes ? bytes : 1) == cudaSuccess ? p : NULL;
 }
 VC_API void vcg_free_host(void *p) {
+    VCD_SCOPE();
     if (p) cudaFreeHost(p);
 }
 VC_API int vcg_copy(void *dst, const void *src, size_t bytes) {
+    VCD_SCOPE();
     if (vcd_init() != 0) return 4;
     return cudaMemcpy(dst, src, bytes, cudaMemcpyDefault) == cudaSuccess ? 0 : 4;
 }
 VC_API int vcg_memset(void *dst, int v, size_t bytes) {
+    VCD_SCOPE();
     if (vcd_init() != 0) return 4;
     return cudaMemset(dst, v, bytes) == cudaSuccess ? 0 : 4;
 }
 VC_API int vcg_sync(void) {
+    VCD_SCOPE();
     if (vcd_init() != 0) return 4;
     vcd_ctx *c = vcd_thread_ctx();
     if (c) cudaStreamSynchronize(c->stream);
     return cudaDeviceSynchronize() == cudaSuccess ? 0 : 4;
 }
 VC_API int vcg_device_info(int *num_sms, int *cc_major, int *cc_minor) {
+    VCD_SCOPE();
     if (vcd_init() != 0) return 4;
     cudaDeviceProp p;
     if (cudaGetDeviceProperties(&p, g_dev.device) != cudaSuccess) return 4;
@@ -182,8 +191,18 @@ VC_API int vcg_device_info(int *num_sms, int *cc_major, int *cc_minor) {
     return 0;
 }
 VC_API const char *vcg_last_error(void) { return vcd_last_error(); }
+VC_API int vcg_device_memory(size_t *free_bytes, size_t *total_bytes) {
+    VCD_SCOPE();
+    if (vcd_init() != 0) return 4;
+    size_t f = 0, t = 0;
+    if (cudaMemGetInfo(&f, &t) != cudaSuccess) return 4;
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return 0;
+}
 
 VC_API int vcg_synth_volume_device(uint32_t nx, uint32_t ny, uint32_t nz, uint64_t seed, uint8_t *out_dev) {
+    VCD_SCOPE();
     if (!nx || !ny || !nz || !out_dev) return 2;
     syn_cfg *c = (syn_cfg *)calloc(1, sizeof(syn_cfg));
     if (!c) return 3;

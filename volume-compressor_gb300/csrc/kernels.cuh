@@ -115,4 +115,9 @@ void launch_idct(const DecodeJob &J, int num_sms, cudaStream_t s, uint64_t t_lo,
 void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s);
 void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cudaStream_t s);
 
+// cudaFuncAttributeMaxDynamicSharedMemorySize of kernel fn, set on the calling
+// thread's current device. The attribute belongs to the device's context, not
+// to the process, so it is set once per (kernel, device) pair.
+cudaError_t smem_attr(const void *fn, int bytes);
+
 }  // namespace vcg

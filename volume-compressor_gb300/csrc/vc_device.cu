@@ -50,13 +50,33 @@ static void init_once(void) {
         return;
     }
     free(t);
-    g_init_rc = 0;
+    __atomic_store_n(&g_init_rc, 0, __ATOMIC_RELEASE);
+}
+
+static void make_current(void) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != g_dev.device) cudaSetDevice(g_dev.device);
 }
 
 extern "C" int vcd_init(void) {
     pthread_once(&g_once, init_once);
-    if (g_init_rc == 0) cudaSetDevice(g_dev.device);
+    if (g_init_rc == 0) make_current();
     return g_init_rc;
+}
+
+extern "C" int vcd_enter(void) {
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    if (__atomic_load_n(&g_init_rc, __ATOMIC_ACQUIRE) == 0 && prev != g_dev.device) cudaSetDevice(g_dev.device);
+    return prev;
+}
+
+extern "C" void vcd_leave(int *prev) {
+    int cur = -1;
+    if (*prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != *prev) cudaSetDevice(*prev);
 }
 
 // ---------------------------------------------------------------- per-thread context
@@ -151,6 +171,40 @@ extern "C" __attribute__((visibility("default"))) int vcg_profile_read(void *out
 extern "C" __attribute__((visibility("default"))) double vcg_last_call_ms(void) {
     vcd_ctx *c = vcd_thread_ctx();
     return c ? c->last_ms : -1.0;
+}
+
+// Dynamic shared-memory limits already raised, per kernel: bit d of devs is
+// device d (devices from 64 up are set on every call).
+namespace {
+struct SmemAttr {
+    const void *fn;
+    int bytes;
+    uint64_t devs;
+};
+SmemAttr g_smem_attr[32];
+int g_n_smem_attr;
+pthread_mutex_t g_smem_mu = PTHREAD_MUTEX_INITIALIZER;
+}  // namespace
+
+cudaError_t vcg::smem_attr(const void *fn, int bytes) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    pthread_mutex_lock(&g_smem_mu);
+    int i = 0;
+    while (i < g_n_smem_attr && (g_smem_attr[i].fn != fn || g_smem_attr[i].bytes != bytes)) ++i;
+    if (i < g_n_smem_attr && bit && (g_smem_attr[i].devs & bit)) {
+        pthread_mutex_unlock(&g_smem_mu);
+        return cudaSuccess;
+    }
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && bit) {
+        if (i == g_n_smem_attr && g_n_smem_attr < 32) g_smem_attr[g_n_smem_attr++] = SmemAttr{fn, bytes, 0};
+        if (i < g_n_smem_attr) g_smem_attr[i].devs |= bit;
+    }
+    pthread_mutex_unlock(&g_smem_mu);
+    return e;
 }
 
 // Range-decoder policy of the plain decode path (rc_lanes_for).
@@ -351,7 +405,10 @@ static cudaError_t copy_out_pageable(vcd_ctx *c, uint8_t *dst, const uint8_t *sr
     void *pin = NULL;
     cudaError_t e = vcd_pinned(c, kBounceChunk * kBounceRing, &pin);
     if (e != cudaSuccess || !vcd_side_stream(c)) {   // the slot events live with the second stream
-        if (e == cudaSuccess && nslab) e = cudaStreamSynchronize(c->stream);
+        // no pinned ring (or no second stream): one plain copy after the work that writes the source
+        cudaGetLastError();
+        e = cudaStreamSynchronize(c->stream);
+        if (e == cudaSuccess && cs != c->stream) e = cudaStreamSynchronize(cs);
         if (e == cudaSuccess) e = cudaMemcpy(dst, src_dev, bytes, cudaMemcpyDeviceToHost);
         return e;
     }
@@ -465,8 +522,12 @@ static void *bounce_in_worker(void *p) {
 static cudaError_t copy_in_pageable(vcd_ctx *c, uint8_t *dst_dev, const uint8_t *src, size_t bytes) {
     void *pin = NULL;
     cudaError_t e = vcd_pinned(c, kBounceChunk * kBounceRing, &pin);
-    if (e != cudaSuccess || !vcd_side_stream(c))   // the slot events live with the second stream
-        return e != cudaSuccess ? e : cudaMemcpy(dst_dev, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess || !vcd_side_stream(c)) {   // the slot events live with the second stream
+        // no pinned ring (or no second stream): one staged copy in stream order
+        cudaGetLastError();
+        e = cudaMemcpyAsync(dst_dev, src, bytes, cudaMemcpyHostToDevice, c->stream);
+        return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+    }
     BounceIn b;
     memset(&b, 0, sizeof b);
     b.c = c; b.dst = dst_dev; b.src = src; b.ring = (uint8_t *)pin; b.bytes = bytes;

@@ -235,6 +235,7 @@ VC_API vc_status vcg_memory_read(void *ud, uint64_t off, uint32_t len, uint8_t *
 }
 
 VC_API void vc_close(vc_archive *a) {
+    VCD_SCOPE();
     if (!a) return;
     if (a->dev) vcd_free_archive(a->dev);
     if (a->sdev) vcd_free_archive(a->sdev);
@@ -702,6 +703,7 @@ static vc_status decode_box(vc_archive *a, int lod, vc_box b, uint8_t *out, uint
 }
 
 VC_API vc_status vc_decode_region(vc_archive *a, int lod, vc_box b, uint8_t *out) {
+    VCD_SCOPE();
     if (!a || lod < 0 || lod >= a->nlod || !out) return VC_ERR_RANGE;
     vc_dims d = lod_dims_of(a->d0, lod);
     if (b.x1 > d.nx || b.y1 > d.ny || b.z1 > d.nz) return VC_ERR_RANGE;
@@ -710,6 +712,7 @@ VC_API vc_status vc_decode_region(vc_archive *a, int lod, vc_box b, uint8_t *out
 }
 
 VC_API vc_status vc_decode_atom(vc_archive *a, int lod, int ax, int ay, int az, uint8_t out[VC_ATOM3]) {
+    VCD_SCOPE();
     if (!a || lod < 0 || lod >= a->nlod || !out) return VC_ERR_RANGE;
     vc_dims d = lod_dims_of(a->d0, lod);
     if ((uint32_t)ax >= (d.nx + 31) / 32 || (uint32_t)ay >= (d.ny + 31) / 32 || (uint32_t)az >= (d.nz + 31) / 32)
@@ -722,6 +725,7 @@ VC_API vc_status vc_decode_atom(vc_archive *a, int lod, int ax, int ay, int az, 
 }
 
 VC_API vc_status vc_decode_lod(vc_archive *a, int lod, uint8_t *out_vol, vc_dims *out_dims) {
+    VCD_SCOPE();
     vc_dims d;
     vc_status s = vc_lod_dims(a, lod, &d);
     if (s != VC_OK) return s;
@@ -732,6 +736,7 @@ VC_API vc_status vc_decode_lod(vc_archive *a, int lod, uint8_t *out_vol, vc_dims
 
 // Device-output variants (include/vcg.h).
 VC_API vc_status vcg_decode_region_device(vc_archive *a, int lod, vc_box b, uint8_t *out_dev) {
+    VCD_SCOPE();
     if (!a || lod < 0 || lod >= a->nlod || !out_dev) return VC_ERR_RANGE;
     vc_dims d = lod_dims_of(a->d0, lod);
     if (b.x1 > d.nx || b.y1 > d.ny || b.z1 > d.nz) return VC_ERR_RANGE;
@@ -740,6 +745,7 @@ VC_API vc_status vcg_decode_region_device(vc_archive *a, int lod, vc_box b, uint
 }
 
 VC_API vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev, vc_dims *out_dims) {
+    VCD_SCOPE();
     vc_dims d;
     vc_status s = vc_lod_dims(a, lod, &d);
     if (s != VC_OK) return s;
@@ -757,6 +763,7 @@ VC_API vc_status vcg_decode_lod_device(vc_archive *a, int lod, uint8_t *out_dev,
 
 VC_API vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_request *reqs, int out_on_device,
                                     vc_status *status) {
+    VCD_SCOPE();
     if (!a || (n && (!reqs || !status))) return VC_ERR_RANGE;
     if (n == 0) return VC_OK;
     if (make_resident(a) != 0) return VC_ERR_IO;
@@ -883,6 +890,7 @@ done:
 }
 
 VC_API vc_status vcg_make_resident(vc_archive *a) {
+    VCD_SCOPE();
     if (!a) return VC_ERR_RANGE;
     return make_resident(a) == 0 ? VC_OK : VC_ERR_IO;
 }
@@ -935,16 +943,19 @@ static vc_status encode_common(const uint8_t *vol, int on_device, vc_dims dims, 
 
 VC_API vc_status vc_encode(const uint8_t *vol, vc_dims dims, float target_ratio, uint8_t **out_archive,
                            size_t *out_len) {
+    VCD_SCOPE();
     return encode_common(vol, 0, dims, target_ratio, NULL, out_archive, out_len, NULL, VCG_DS_BOX, 0.0f);
 }
 
 VC_API vc_status vcg_encode_device(const uint8_t *vol_dev, vc_dims dims, float target_ratio,
                                    uint8_t **out_archive, size_t *out_len, float *q0) {
+    VCD_SCOPE();
     return encode_common(vol_dev, 1, dims, target_ratio, NULL, out_archive, out_len, q0, VCG_DS_BOX, 0.0f);
 }
 
 VC_API vc_status vcg_encode_q(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
                               const float base_q[VC_NLOD], uint8_t **out_archive, size_t *out_len) {
+    VCD_SCOPE();
     if (!base_q) return VC_ERR_RANGE;
     return encode_common(vol, vol_on_device, dims, target_ratio, base_q, out_archive, out_len, NULL, VCG_DS_BOX, 0.0f);
 }
@@ -956,6 +967,7 @@ static int ds_args_ok(int method, float alpha) {
 VC_API vc_status vcg_encode_ds(const uint8_t *vol, int vol_on_device, vc_dims dims, float target_ratio,
                                const float base_q[VC_NLOD], int method, float alpha, uint8_t **out_archive,
                                size_t *out_len) {
+    VCD_SCOPE();
     if (!ds_args_ok(method, alpha)) return VC_ERR_RANGE;
     return encode_common(vol, vol_on_device, dims, target_ratio, base_q, out_archive, out_len, NULL, method, alpha);
 }
@@ -978,6 +990,7 @@ static vc_status downscale_common(const uint8_t *in, int on_device, vc_dims d, i
 
 VC_API vc_status vcg_downscale2x(const uint8_t *in, int on_device, vc_dims dims, int method, float alpha, uint8_t *out,
                                  vc_dims *out_dims) {
+    VCD_SCOPE();
     if (out_dims) {
         out_dims->nx = (dims.nx + 1) / 2;
         out_dims->ny = (dims.ny + 1) / 2;
@@ -988,6 +1001,7 @@ VC_API vc_status vcg_downscale2x(const uint8_t *in, int on_device, vc_dims dims,
 
 VC_API vc_status vcg_downscale_pyramid(const uint8_t *vol_dev, vc_dims dims, int method, float alpha, int levels,
                                        uint8_t *const *out_dev) {
+    VCD_SCOPE();
     return downscale_common(vol_dev, 1, dims, method, alpha, levels, out_dev);
 }
 
@@ -1058,6 +1072,7 @@ vc_status vch_view_decode_2x2x2(vc_archive *a, int lod, uint32_t az0, uint32_t a
 // The image is assembled on the device from the resident archive.
 // ---------------------------------------------------------------------------
 VC_API vc_status vcg_repack_v2(vc_archive *a, uint8_t **out_archive, size_t *out_len) {
+    VCD_SCOPE();
     if (!a || !out_archive || !out_len) return VC_ERR_RANGE;
     *out_archive = NULL;
     *out_len = 0;

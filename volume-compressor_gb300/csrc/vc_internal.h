@@ -88,7 +88,14 @@ typedef struct {
 typedef struct vcd_archive vcd_archive;   // device residency of one archive
 
 // ---- device layer (vc_device.cu) ------------------------------------------
-int  vcd_init(void);                        // 0 ok; -1 no usable device
+int  vcd_init(void);                        // 0 ok; -1 no usable device; makes the library's device current
+// The library runs on one device (VC_DEVICE, default 0). A public entry point
+// that uses the GPU opens with VCD_SCOPE(): the library's device is made current
+// for the call (once the library is initialised; the first vcd_init selects it)
+// and the caller's current device is current again when the call returns.
+int  vcd_enter(void);                       // the caller's current device, or -1
+void vcd_leave(int *prev);
+#define VCD_SCOPE() int vcd_prev_ __attribute__((cleanup(vcd_leave))) = vcd_enter()
 const char *vcd_last_error(void);
 // residency: begin starts the copy of the archive bytes, finish adds the atom
 // table and the dequantisation tables and waits (the caller frees on failure)

@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include "kernels.cuh"
+#include "vc_device.h"
 
 using namespace vcg;
 
@@ -63,6 +64,7 @@ static int na_setup(int dev, uint8_t **base, int *sms) {
         }
         if (e != cudaSuccess) {
             pthread_mutex_unlock(&g_na_mu);
+            vcd_set_error("no-alloc decode: scratch set-up", e);
             return e == cudaErrorMemoryAllocation ? 3 : 4;
         }
         g_na_sms[dev] = n;
@@ -103,7 +105,11 @@ VC_API int vcg_decode_atoms_noalloc(const uint8_t *payload_dev, size_t payload_b
         atoms[i].len = lengths[i];
     }
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return 4;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) {
+        vcd_set_error("no-alloc decode: current device", e);
+        return 4;
+    }
     uint8_t *base = NULL;
     int sms = 0;
     int rc = na_setup(dev, &base, &sms);
@@ -111,11 +117,14 @@ VC_API int vcg_decode_atoms_noalloc(const uint8_t *payload_dev, size_t payload_b
     vcd_dq dq;
     vch_dq_consts(base_q, &dq);
     cudaStream_t st = cudaStreamPerThread;
-    cudaError_t e = cudaMemcpyAsync(base + kNaAtoms, atoms, n_atoms * sizeof(vcd_atom), cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(base + kNaAtoms, atoms, n_atoms * sizeof(vcd_atom), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + kNaDq, &dq, sizeof dq, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(base + kNaCtl, 0, 16, st);          // entry total starts at zero
     if (e == cudaSuccess) e = cudaMemsetAsync(base + kNaCtl, 0xFF, 4, st);        // no malformed atom yet
-    if (e != cudaSuccess) return 4;
+    if (e != cudaSuccess) {
+        vcd_set_error("no-alloc decode: upload of the atom table", e);
+        return 4;
+    }
     DecodeJob J;
     memset(&J, 0, sizeof J);
     J.arc = payload_dev;
@@ -136,10 +145,20 @@ VC_API int vcg_decode_atoms_noalloc(const uint8_t *payload_dev, size_t payload_b
     J.nnz_total = reinterpret_cast<unsigned long long *>(base + kNaCtl + 8);
     memcpy(J.band_start, g_na_band, sizeof J.band_start);
     launch_decode_lists(J, sms, st);
+    if ((e = cudaGetLastError()) != cudaSuccess) {   // the launches of this call
+        vcd_set_error("no-alloc decode: kernel launch", e);
+        return 4;
+    }
     uint32_t err = 0xFFFFFFFFu;
     e = cudaMemcpyAsync(&err, base + kNaCtl, 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaGetLastError();
-    if (e != cudaSuccess) return 4;
-    return err < n_atoms ? 1 : 0;
+    if (e != cudaSuccess) {
+        vcd_set_error("no-alloc decode", e);
+        return 4;
+    }
+    if (err < n_atoms) {
+        vcd_set_error("no-alloc decode: malformed payload", cudaSuccess);
+        return 1;
+    }
+    return 0;
 }

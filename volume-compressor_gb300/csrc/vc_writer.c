@@ -368,6 +368,7 @@ static vc_status submit(vc_writer *w, wreq *r) {
 // ---------------------------------------------------------------- API
 
 VC_API vc_writer *vc_create(const char *path, vc_dims lod0_dims, float target_ratio) {   // src/vc/vc.c:995-1073
+    VCD_SCOPE();
     if (!path || !dims_ok(lod0_dims) || target_ratio < 1.0f) return NULL;
     int nlod = 1;
     for (int l = 1; l < VC_NLOD; ++l) {
@@ -422,6 +423,7 @@ VC_API vc_writer *vc_create(const char *path, vc_dims lod0_dims, float target_ra
 }
 
 VC_API vc_status vc_set_base_q(vc_writer *w, int lod, float q) {   // src/vc/vc.c:1075-1080
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod || isnan(q)) return VC_ERR_RANGE;
     if (q < 0.05f) q = 0.05f;
     if (q > 4096.0f) q = 4096.0f;
@@ -439,6 +441,7 @@ VC_API vc_status vc_set_base_q(vc_writer *w, int lod, float q) {   // src/vc/vc.
 
 VC_API vc_status vc_append_atom(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax,
                                 const uint8_t vox[VC_ATOM3]) {   // src/vc/vc.c:1161-1168
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod || !vox) return VC_ERR_RANGE;
     const vc_dims d = lod_dims(w->d0, lod);
     if (ax >= (d.nx + 31) / 32 || ay >= (d.ny + 31) / 32 || az >= (d.nz + 31) / 32) return VC_ERR_RANGE;
@@ -451,6 +454,7 @@ VC_API vc_status vc_append_atom(vc_writer *w, int lod, uint32_t az, uint32_t ay,
 }
 
 VC_API vc_status vc_append_box(vc_writer *w, int lod, vc_box b, const uint8_t *voxels) {   // src/vc/vc.c:1170-1189
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod || !voxels) return VC_ERR_RANGE;
     if (b.x0 % 32 || b.y0 % 32 || b.z0 % 32) return VC_ERR_RANGE;
     if ((b.x1 - b.x0) % 32 || (b.y1 - b.y0) % 32 || (b.z1 - b.z0) % 32) return VC_ERR_RANGE;
@@ -465,6 +469,7 @@ VC_API vc_status vc_append_box(vc_writer *w, int lod, vc_box b, const uint8_t *v
 
 VC_API vc_status vcg_append_atom_async(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax,
                                        const uint8_t vox[VC_ATOM3]) {
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod || !vox) return VC_ERR_RANGE;
     const vc_dims d = lod_dims(w->d0, lod);
     if (ax >= (d.nx + 31) / 32 || ay >= (d.ny + 31) / 32 || az >= (d.nz + 31) / 32) return VC_ERR_RANGE;
@@ -485,6 +490,7 @@ VC_API vc_status vcg_append_atom_async(vc_writer *w, int lod, uint32_t az, uint3
 }
 
 VC_API vc_status vcg_writer_flush(vc_writer *w, uint64_t *failed) {
+    VCD_SCOPE();
     if (failed) *failed = 0;
     if (!w) return VC_ERR_RANGE;
     wreq r;
@@ -500,6 +506,7 @@ VC_API vc_status vcg_writer_flush(vc_writer *w, uint64_t *failed) {
 }
 
 VC_API vc_status vc_mark_zero_atom(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax) {   // :1191-1205
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod) return VC_ERR_RANGE;
     pthread_mutex_lock(&w->mu);
     pthread_rwlock_wrlock(&w->rw);
@@ -514,6 +521,7 @@ VC_API vc_status vc_mark_zero_atom(vc_writer *w, int lod, uint32_t az, uint32_t 
 }
 
 VC_API vc_status vc_mark_zero_region(vc_writer *w, int lod, uint32_t rz, uint32_t ry, uint32_t rx) {   // :1207-1229
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod) return VC_ERR_RANGE;
     pthread_mutex_lock(&w->mu);
     pthread_rwlock_wrlock(&w->rw);
@@ -533,6 +541,7 @@ VC_API vc_status vc_mark_zero_region(vc_writer *w, int lod, uint32_t rz, uint32_
 
 VC_API vc_status vc_writer_decode_atom(vc_writer *w, int lod, uint32_t az, uint32_t ay, uint32_t ax,
                                        uint8_t out[VC_ATOM3]) {   // src/vc/vc.c:1484-1493
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod || !out) return VC_ERR_RANGE;
     pthread_rwlock_rdlock(&w->rw);
     const vc_status s = vc_decode_atom(w->view, lod, (int)ax, (int)ay, (int)az, out);
@@ -550,6 +559,7 @@ VC_API vc_cover vc_writer_coverage(vc_writer *w, int lod, uint32_t az, uint32_t 
 
 VC_API vc_status vc_writer_decode_2x2x2(vc_writer *w, int lod, uint32_t az0, uint32_t ay0, uint32_t ax0,
                                         uint8_t out8[8][VC_ATOM3], int *any) {   // src/vc/vc.c:1507-1530
+    VCD_SCOPE();
     if (!w || lod < 0 || lod >= w->nlod || !out8) return VC_ERR_RANGE;
     pthread_rwlock_rdlock(&w->rw);
     const vc_status s = vch_view_decode_2x2x2(w->view, lod, az0, ay0, ax0, out8, any);
@@ -558,6 +568,7 @@ VC_API vc_status vc_writer_decode_2x2x2(vc_writer *w, int lod, uint32_t az0, uin
 }
 
 VC_API void vc_writer_close(vc_writer *w) {   // src/vc/vc.c:1231-1245
+    VCD_SCOPE();
     if (!w) return;
     vcg_writer_flush(w, NULL);   // asynchronous appends still queued
     pthread_mutex_lock(&w->mu);

@@ -32,7 +32,7 @@ VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_re
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
-               "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_last_error", "vcg_profile_enable",
+               "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_device_memory", "vcg_last_error", "vcg_profile_enable",
                "vcg_profile_read", "vcg_last_call_ms"]
 
 
@@ -190,6 +190,7 @@ def lib():
         L.vcg_copy.argtypes = [P, P, ctypes.c_size_t]
         L.vcg_memset.argtypes = [P, ctypes.c_int, ctypes.c_size_t]
         L.vcg_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+        L.vcg_device_memory.argtypes = [ctypes.POINTER(ctypes.c_size_t)] * 2
         L.vcg_last_error.restype = ctypes.c_char_p
         L.vcg_decode_atoms_noalloc.argtypes = [P, ctypes.c_size_t, P, P, ctypes.c_uint32, ctypes.c_float, P]
         L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
@@ -291,6 +292,13 @@ def device_info():
     a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     s = lib().vcg_device_info(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
     return s, a.value, (b.value, c.value)
+
+
+def device_memory():
+    """(status, free bytes, total bytes) of the library's device (cudaMemGetInfo)."""
+    f, t = ctypes.c_size_t(), ctypes.c_size_t()
+    s = lib().vcg_device_memory(ctypes.byref(f), ctypes.byref(t))
+    return s, f.value, t.value
 
 
 # ---------------------------------------------------------------- codec
