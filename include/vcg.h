@@ -49,11 +49,12 @@ vc_status vcg_set_batch_shape(int rc_scalar_warps, int transform_threads, int tr
 
 // Range-decoder policy of vc_decode_region / vc_decode_lod / vc_decode_atom and
 // the device-output variants (process-wide; results do not depend on it). A
-// warp that decodes one atom has the lowest latency per atom; warps of 2..32
-// atoms decoded in lockstep have the highest throughput. Atoms are decoded one
-// per warp while that makes at most w warps per SM sub-partition (4 per SM),
-// else in warps of the smallest power of two that keeps to about one warp per
-// sub-partition. w <= 0 restores the default (16).
+// warp that decodes one atom has the lowest latency per atom; the per-lane
+// decoder (every lane of a warp decodes its own atom, the atoms put in order of
+// payload length first) has the highest throughput. Atoms are decoded one per
+// warp while that makes at most w warps per SM sub-partition (4 per SM), else
+// by the per-lane decoder. w = 0: always the per-lane decoder; w < 0 restores
+// the default (16).
 void vcg_set_rc_scalar_warps(int w);
 
 // Decode server: continuous batching against one resident archive. Requests

@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 from conftest import load_archive
+from rcstream import hostile_payload
 
 pytestmark = pytest.mark.gpu
 
@@ -65,72 +66,6 @@ def test_noalloc_rejects_more_than_its_limit(vc, gpu):
         vc.VC_ERR_FORMAT
 
 
-class _RangeEncoder:
-    """Binary range encoder with the codec's arithmetic (12-bit probabilities of
-    a zero bit, shift-5 adaptation, bypass bits halve the range, five flush
-    shifts; src/vc/vc.c:344-401). Used only to craft a payload that no
-    encoder of the codec would write."""
-
-    def __init__(self):
-        self.low, self.range, self.cache, self.pending, self.out = 0, 0xFFFFFFFF, 0, 1, bytearray()
-
-    def _shift(self):
-        if (self.low & 0xFFFFFFFF) < 0xFF000000 or (self.low >> 32):
-            carry, b = self.low >> 32, self.cache
-            while True:
-                self.out.append((b + carry) & 0xFF)
-                b = 0xFF
-                self.pending -= 1
-                if not self.pending:
-                    break
-            self.cache = (self.low >> 24) & 0xFF
-        self.pending += 1
-        self.low = (self.low & 0x00FFFFFF) << 8
-
-    def _norm(self):
-        while self.range < (1 << 24):
-            self._shift()
-            self.range = (self.range << 8) & 0xFFFFFFFF
-
-    def bit(self, ctx, i, b):
-        r0 = (self.range * ctx[i]) >> 12
-        if b:
-            self.low += r0
-            self.range -= r0
-            ctx[i] -= ctx[i] >> 5
-        else:
-            self.range = r0
-            ctx[i] += (4096 - ctx[i]) >> 5
-        self._norm()
-
-    def bypass(self, b):
-        self.range >>= 1
-        if b:
-            self.low += self.range
-        self._norm()
-
-    def finish(self):
-        for _ in range(5):
-            self._shift()
-        return bytes(self.out)
-
-
-def _hostile_payload(dc=100, prefix_ones=40):
-    """[dc][coder bytes] of a stream whose first coefficient escapes with an
-    exponential-Golomb prefix of `prefix_ones` ones: longer than any level can
-    need, so a decoder must reject it as malformed."""
-    e = _RangeEncoder()
-    sig, mag = [2048] * 8, [2048] * 12
-    for i in range(15, -1, -1):   # EOB = 1
-        e.bypass((1 >> i) & 1)
-    e.bit(sig, 0, 1)              # scan position 0 (band 0) is significant
-    for k in range(12):           # unary magnitude saturates, then the escape
-        e.bit(mag, k, 1)
-    for _ in range(prefix_ones):
-        e.bypass(1)
-    return bytes([dc]) + e.finish()
-
-
 def _payloads(a, data, lod, atoms):
     offs = np.zeros(len(atoms), np.uint64)
     lens = np.zeros(len(atoms), np.uint32)
@@ -145,7 +80,7 @@ def test_noalloc_rejects_a_malformed_payload_then_decodes_correctly(vc, oracle, 
     VC_ERR_FORMAT (the oracle rejects it too); the scratch it leaves behind must
     not change the next, correct call, which still equals vc_decode_atom."""
     data = load_archive(golden["synth_prime_97x131x65_t20"])
-    bad = _hostile_payload()
+    bad = hostile_payload()
     out = np.zeros(32768, np.uint8)
     assert oracle.lib().orc_decode_atom_payload(bad, len(bad), ctypes.c_float(1.0), vc.ptr(out)) == 1
     a = vc.Archive(data)

@@ -131,8 +131,121 @@ __global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G) {
     if (bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
 }
 
+// ---- per-lane decoder (RcLane) for large decodes. The atoms are first put in
+// order of payload length, longest first (a counting sort on length / 32), so
+// that the 32 atoms of a warp need about the same number of steps: a warp
+// runs until its slowest lane is done.
+__device__ __forceinline__ uint32_t len_bucket(uint32_t len) {
+    const uint32_t k = len >> 5;
+    return kSortBuckets - 1u - (k < kSortBuckets - 1u ? k : kSortBuckets - 1u);
+}
+
+__global__ void k_len_hist(DecodeJob J) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J.n_atoms) return;
+    uint32_t az, ay, ax;
+    box_atom(J, t, az, ay, ax);
+    const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
+    if (e.kind == VCD_PRESENT) atomicAdd(&J.sort_ctl[len_bucket(e.len)], 1u);
+}
+
+// exclusive scan of the kSortBuckets counters in place; their sum -> ctl[kSortBuckets]
+__global__ void __launch_bounds__(1024) k_len_scan(uint32_t *ctl) {
+    __shared__ uint32_t warp_sum[32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
+    uint32_t a[4], s = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        a[j] = s;
+        s += ctl[tid * 4 + j];
+    }
+    uint32_t incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) warp_sum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t w = warp_sum[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+            if (lane >= (uint32_t)o) wi += y;
+        }
+        warp_sum[lane] = wi - w;
+        if (lane == 31) ctl[kSortBuckets] = wi;
+    }
+    __syncthreads();
+    const uint32_t base = warp_sum[wid] + incl - s;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ctl[tid * 4 + j] = base + a[j];
+}
+
+__global__ void k_len_scatter(DecodeJob J) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J.n_atoms) return;
+    uint32_t az, ay, ax;
+    box_atom(J, t, az, ay, ax);
+    const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
+    if (e.kind == VCD_PRESENT) J.order[atomicAdd(&J.sort_ctl[len_bucket(e.len)], 1u)] = (uint32_t)t;
+}
+
+static_assert(kSortBuckets == 4 * 1024, "k_len_scan: 1024 threads x 4 counters");
+
+constexpr int kLaneThreads = 64;   // 2 warps per CTA
+constexpr int kLaneUnroll = 8;     // steps between warp votes
+
+__global__ void __launch_bounds__(kLaneThreads) k_rc_lanes(DecodeJob J) {
+    __shared__ uint32_t bstart[9];
+    __shared__ uint32_t S[12 * kLaneThreads];   // magnitude contexts, lane-interleaved
+    if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
+    __syncthreads();
+    const uint64_t i = (uint64_t)blockIdx.x * kLaneThreads + threadIdx.x;
+    const bool active = i < J.sort_ctl[kSortBuckets];
+    uint64_t t = 0;
+    vcd_atom e = {};
+    uint32_t cap = 0;
+    uint32_t *dst = J.ent;
+    if (active) {
+        t = J.order[i];
+        uint32_t az, ay, ax;
+        box_atom(J, t, az, ay, ax);
+        e = J.atoms[job_atom(J, t, az, ay, ax)];
+        cap = 8u * (e.len - 1u) + 64u;
+        if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+        dst = J.ent + J.ent_off[t];
+    }
+    uint32_t *Sl = S + threadIdx.x;
+    RcLane L;
+    L.init(J.arc + e.off + 1, e.len - 1u, active, bstart, Sl, kLaneThreads, dst, cap);
+    while (__any_sync(0xFFFFFFFFu, L.c != kLaneDone)) {
+#pragma unroll
+        for (int k = 0; k < kLaneUnroll; ++k) L.step(bstart, Sl, kLaneThreads);
+    }
+    if (!active) return;
+    const uint32_t n = L.n > cap ? cap : L.n;
+    J.cnt[t] = n | (L.n > cap ? kEntOverflow : 0u) | (L.bad ? kEntBad : 0u);
+    atomicAdd(J.nnz_total, (unsigned long long)n);
+    if (L.bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
+}
+
+// The range decode of every PRESENT box atom: above rc_scalar_warps() atoms per
+// SM sub-partition (and with an order buffer) the per-lane decoder over atoms
+// sorted by payload length, else one atom per warp (scalar decoder).
 static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s) {
     const uint32_t G = rc_lanes_for(J.n_atoms, (uint32_t)num_sms, rc_scalar_warps());
+    if (G > 1 && J.order && J.sort_ctl) {
+        const unsigned nb = (unsigned)((J.n_atoms + 255) / 256);
+        cudaMemsetAsync(J.sort_ctl, 0, sort_ctl_words() * 4, s);
+        k_len_hist<<<nb, 256, 0, s>>>(J);
+        k_len_scan<<<1, 1024, 0, s>>>(J.sort_ctl);
+        k_len_scatter<<<nb, 256, 0, s>>>(J);
+        k_rc_lanes<<<(unsigned)((J.n_atoms + kLaneThreads - 1) / kLaneThreads), kLaneThreads, 0, s>>>(J);
+        return;
+    }
     k_rc_decode<<<(unsigned)((J.n_atoms + G - 1) / G), 32, 0, s>>>(J, G);
 }
 

@@ -32,7 +32,12 @@ struct DecodeJob {
     uint32_t band_start[9];      // first scan position of each significance band
     uint64_t t_lo, t_hi;         // box atoms the inverse transform launch covers
     uint32_t box_table;          // 1: atoms[] is indexed by box atom (staged decode), 0: by LOD raster
+    // per-lane range decoder of large decodes (optional; NULL: the warp decoders):
+    uint32_t *order;             // n_atoms slots: PRESENT box atoms, longest payload first
+    uint32_t *sort_ctl;          // kSortBuckets counters + present-atom count
 };
+constexpr uint32_t kSortBuckets = 4096;   // payload length / 32, clamped
+__host__ __device__ inline size_t sort_ctl_words() { return kSortBuckets + 4; }
 
 __host__ __device__ inline uint64_t job_atom(const DecodeJob &J, uint64_t t, uint32_t az, uint32_t ay,
                                              uint32_t ax) {
@@ -99,6 +104,7 @@ __host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms,
     return g < 2 ? 2u : (uint32_t)g;
 }
 constexpr uint32_t kRcScalarWarpsDefault = 16;
+
 // policy of the plain decode path (vcg_set_rc_scalar_warps)
 uint32_t rc_scalar_warps();
 // mid (optional): recorded between the range decode and the transform

@@ -278,6 +278,143 @@ __device__ __forceinline__ int rc_decode_levels_warp(const uint8_t *src, uint32_
     return bad ? 1 : 0;
 }
 
+// ---------------------------------------------------------------- per-lane decoder
+// Each lane of a warp decodes its own atom and every step is one binary
+// decision of that atom, whatever its kind: the lanes of a warp are at
+// different points of their streams, and no lane waits for another (unlike the
+// lockstep decoder, whose warps run every magnitude step as long as any lane
+// needs it). The decision kind is the lane's state:
+//   0        significance bit of scan position p (band context, a register)
+//   1..12    unary magnitude step c - 1 (context mag[c - 1] in shared memory)
+//   13       escape: exponential-Golomb prefix of ones (bypass)
+//   14       bypass run: the escape suffix bits, then the sign bit
+//   15       done
+// (src/vc/vc.c:491-506, 545-560). A bypass bit is the adaptive split with
+// probability 2048 and no adaptation, except that the range becomes the half
+// for both bit values (src/vc/vc.c:431-441). The magnitude context of the next
+// step is loaded from shared memory one step ahead. Stream bytes are fetched
+// one at a time, one byte ahead of the renormalisation that consumes them;
+// bytes past the end read as zero. Probabilities are kept unscaled (12 bits).
+__device__ __forceinline__ uint32_t ld_u8_if(bool on, const uint8_t *ptr, uint32_t old) {
+    uint32_t v = old;
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.global.nc.u8 %0, [%1];\n\t}"
+                 : "+r"(v) : "l"(ptr), "r"((uint32_t)on));
+    return v;
+}
+__device__ __forceinline__ void st_u32_if(bool on, uint32_t *ptr, uint32_t v) {
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u32 [%0], %1;\n\t}"
+                 :: "l"(ptr), "r"(v), "r"((uint32_t)on) : "memory");
+}
+
+constexpr uint32_t kLaneDone = 15u;
+
+struct RcLane {
+    const uint8_t *src;
+    uint32_t pos, len;     // next byte to fetch; stream length
+    uint32_t nxt;          // the byte at pos (0 past the end)
+    uint32_t code, range;
+    uint32_t c, r, m;      // state; escape / run count; magnitude so far
+    uint32_t p, eob, bend, bi;   // scan position, EOB, end of the current band, band
+    uint32_t sigp, magp;   // context of the current band; magnitude context of the next step
+    uint32_t *dst;         // coefficient list (scan position | level << 16)
+    uint32_t n, cap, bad;  // entries decoded (all, also past cap); list capacity; malformed
+
+    // S: this lane's 12 magnitude contexts at S[0], S[st], ..., S[11 * st]
+    __device__ __forceinline__ void init(const uint8_t *s, uint32_t l, bool active, const uint32_t *bstart,
+                                         uint32_t *S, uint32_t st, uint32_t *d, uint32_t cp) {
+        src = s;
+        len = active ? l : 0u;
+        uint32_t cd = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < 5; ++i) cd = (cd << 8) | (i < len ? (uint32_t)__ldg(src + i) : 0u);
+        pos = 5;
+        nxt = 5 < len ? __ldg(src + 5) : 0u;
+        uint32_t rg = 0xFFFFFFFFu, e = 0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {   // 16-bit EOB in bypass bits (src/vc/vc.c:520-525)
+            rg >>= 1;
+            const bool b = cd >= rg;
+            cd = b ? cd - rg : cd;
+            e = (e << 1) | (b ? 1u : 0u);
+            if (rg < kTop) {
+                rg <<= 8;
+                cd = (cd << 8) | nxt;
+                ++pos;
+                nxt = pos < len ? __ldg(src + pos) : 0u;
+            }
+        }
+        if (e > 32768u) e = 32768u;   // src/vc/vc.c:549
+        code = cd;
+        range = rg;
+        eob = e;
+        p = 0;
+        bi = 0;
+        bend = bstart[1];
+        sigp = 2048u;
+        magp = 2048u;
+#pragma unroll
+        for (int k = 0; k < 12; ++k) S[k * st] = 2048u;
+        c = (active && e) ? 0u : kLaneDone;
+        r = 0;
+        m = 0;
+        dst = d;
+        n = 0;
+        cap = cp;
+        bad = 0;
+    }
+
+    __device__ __forceinline__ void step(const uint32_t *bstart, uint32_t *S, uint32_t st) {
+        const uint32_t s0 = c;
+        const bool isA = s0 < 13u, isPre = s0 == 13u, isRun = s0 == 14u, isSig = s0 == 0u;
+        const uint32_t nmag = S[(s0 < 11u ? s0 : 11u) * st];   // context of step s0 + 1 if this bit is a one
+        const uint32_t pc = isSig ? sigp : magp;
+        const uint32_t pr = isA ? pc : 2048u;
+        const uint32_t r0 = __umulhi(range, pr << 20);
+        const bool b = code >= r0;
+        const uint32_t one = b ? 1u : 0u;
+        code = b ? code - r0 : code;
+        const uint32_t nr = (b && isA) ? range - r0 : r0;
+        const uint32_t pa = rc_adapt(pc, b);
+        if (s0 - 1u < 12u) S[(s0 - 1u) * st] = pa;
+        sigp = isSig ? pa : sigp;
+        magp = nmag;
+        // renormalisation: one byte at most
+        const bool ren = nr < kTop;
+        range = ren ? nr << 8 : nr;
+        code = ren ? (code << 8) | nxt : code;
+        const uint32_t np_ = pos + (ren ? 1u : 0u);
+        pos = np_;
+        nxt = ld_u8_if(ren && np_ < len, src + np_, ren ? 0u : nxt);
+        // the sign bit ends a run of one: emit the level
+        const uint32_t r_ = r, m_ = m;
+        const bool last = isRun && r_ == 1u;
+        const uint32_t sm = b ? 0u - m_ : m_;
+        st_u32_if(last && n < cap, dst + n, (sm << 16) | p);
+        n += last ? 1u : 0u;
+        // next state: a one climbs the ladder (12 -> 13 is the escape); a zero at
+        // significance moves on, a zero on the ladder ends the magnitude (run of
+        // one: the sign); the prefix ends with a zero (run of ones + 1 bits)
+        const uint32_t cA = b ? s0 + 1u : (isSig ? 0u : 14u);
+        const uint32_t cB = isPre ? 14u - one : (last ? 0u : 14u);
+        uint32_t nc = isA ? cA : (s0 == kLaneDone ? kLaneDone : cB);
+        r = isA ? one ^ 1u : (isPre ? r_ + 1u : r_ - 1u);
+        // magnitude: the ladder step that ended it, or 11 + the suffix value
+        m = isA ? s0 : (isPre ? 12u : 2u * m_ + one - 11u);
+        const bool malformed = isPre && b && r_ == 32u;   // a prefix of 33 ones: no level needs it
+        bad |= malformed ? 1u : 0u;
+        const bool adv = (isSig && !b) || last;
+        const uint32_t pn = p + (adv ? 1u : 0u);
+        p = pn;
+        const bool cross = adv && pn == bend;   // next band: fresh context
+        nc = (malformed || (adv && pn == eob)) ? kLaneDone : nc;
+        const uint32_t nbi = bi + (cross ? 1u : 0u);
+        bi = nbi;
+        bend = cross ? bstart[nbi + 1u] : bend;
+        sigp = cross ? 2048u : sigp;
+        c = nc;
+    }
+};
+
 // ---------------------------------------------------------------- encoder
 // WRITE = false only tracks the interval width: the byte count of the
 // reference encoder equals its number of shift-low calls (renormalisation

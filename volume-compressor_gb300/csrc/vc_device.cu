@@ -211,7 +211,7 @@ cudaError_t vcg::smem_attr(const void *fn, int bytes) {
 static uint32_t g_rc_scalar_warps = vcg::kRcScalarWarpsDefault;
 uint32_t vcg::rc_scalar_warps() { return __atomic_load_n(&g_rc_scalar_warps, __ATOMIC_RELAXED); }
 extern "C" __attribute__((visibility("default"))) void vcg_set_rc_scalar_warps(int w) {
-    const uint32_t v = w <= 0 ? vcg::kRcScalarWarpsDefault : (uint32_t)(w > 64 ? 64 : w);
+    const uint32_t v = w < 0 ? vcg::kRcScalarWarpsDefault : (uint32_t)(w > 64 ? 64 : w);
     __atomic_store_n(&g_rc_scalar_warps, v, __ATOMIC_RELAXED);
 }
 
@@ -610,6 +610,12 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
         return vcd_status_of(e);
     }
     p_err = p_ctl;
+    void *p_ord = NULL;   // only large decodes use the per-lane range decoder (launch_rc)
+    if (rc_lanes_for(n, (uint32_t)g_dev.num_sms, rc_scalar_warps()) > 1 &&
+        (e = vcd_scratch(c, VCD_BUF_ORD, (n + sort_ctl_words()) * 4 + 16, &p_ord)) != cudaSuccess) {
+        vcd_set_error("decode scratch", e);
+        return vcd_status_of(e);
+    }
     if (out_dev) {
         p_out = out_dev;
     } else if ((e = vcd_scratch(c, VCD_BUF_OUT, out_bytes, &p_out)) != cudaSuccess) {
@@ -634,6 +640,10 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     J.err = (uint32_t *)p_err;
     J.nnz_total = (unsigned long long *)((uint8_t *)p_ctl + 8);
     memcpy(J.band_start, g_dev.band_start, sizeof J.band_start);
+    if (p_ord) {
+        J.sort_ctl = (uint32_t *)p_ord;
+        J.order = J.sort_ctl + sort_ctl_words();
+    }
 
     if ((e = cudaMemsetAsync(p_ctl, 0, 16, c->stream)) != cudaSuccess ||
         (e = cudaMemsetAsync(p_err, 0xFF, 4, c->stream)) != cudaSuccess) {
@@ -725,7 +735,8 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     if (vcd_prof_on()) {
         const uint64_t nnz = ctl_h[1];
         vcd_prof_add("decode_place", vcd_elapsed(ev.ev[0], ev.ev[1]), n ? 2 : 0, 24 * n, 8 * n, n);
-        vcd_prof_add("rc_decode", vcd_elapsed(ev.ev[1], ev.ev[2]), n ? 1 : 0, r->payload_bytes + 16 * n, 4 * nnz,
+        // (the per-lane decoder: length sort in three kernels, then the decoder)
+        vcd_prof_add("rc_decode", vcd_elapsed(ev.ev[1], ev.ev[2]), n ? (p_ord ? 4 : 1) : 0, r->payload_bytes + 16 * n, 4 * nnz,
                      r->present);
         vcd_prof_add("idct", vcd_elapsed(ev.ev[2], ev.ev[3]), n ? 1 : 0, 4 * nnz + 16 * n, out_bytes, n);
     }

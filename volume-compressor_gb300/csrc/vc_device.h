@@ -13,6 +13,7 @@ enum {
     VCD_BUF_BUA, VCD_BUF_BDST, VCD_BUF_BREQ, VCD_BUF_BOFF, VCD_BUF_BCNT, VCD_BUF_BENT, VCD_BUF_BCTL, VCD_BUF_BOUT,
     VCD_BUF_BPIN, VCD_BUF_COEF, VCD_BUF_RPK, VCD_BUF_RPKREC, VCD_BUF_STG, VCD_BUF_WPACK,
     VCD_BUF_EENT2, VCD_BUF_EMETA2,   // encode: lists and metadata of the coarser LODs (second stream)
+    VCD_BUF_ORD,                     // decode: atom order of the per-lane range decoder + sort counters
     VCD_NBUF
 };
 
