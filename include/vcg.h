@@ -48,13 +48,14 @@ void vcg_batch_shape(int *rc_scalar_warps, int *transform_threads, int *transfor
 vc_status vcg_set_batch_shape(int rc_scalar_warps, int transform_threads, int transform_imma);
 
 // Range-decoder policy of vc_decode_region / vc_decode_lod / vc_decode_atom and
-// the device-output variants (process-wide; results do not depend on it). A
-// warp that decodes one atom has the lowest latency per atom; the per-lane
-// decoder (every lane of a warp decodes its own atom, the atoms put in order of
-// payload length first) has the highest throughput. Atoms are decoded one per
-// warp while that makes at most w warps per SM sub-partition (4 per SM), else
-// by the per-lane decoder. w = 0: always the per-lane decoder; w < 0 restores
-// the default (16).
+// the device-output variants (process-wide; results do not depend on it). Up
+// to one atom per SM sub-partition (4 per SM) each atom has a warp running the
+// latency-tuned scalar decoder; up to w warps per sub-partition, one atom per
+// warp with the plain scalar decoder, longest payloads first; above that the
+// per-lane decoder (every lane of a warp decodes its own atom, atoms in order
+// of payload length). w = 0: always the per-lane decoder; w < 0 restores the
+// default (8: measured on GB300, the per-lane decoder wins from 3,000-5,000
+// atoms on, depending on the atoms' sizes).
 void vcg_set_rc_scalar_warps(int w);
 
 // Decode server: continuous batching against one resident archive. Requests

@@ -88,15 +88,21 @@ __global__ void __launch_bounds__(1024) k_scan_u64(uint64_t *v, uint64_t n, uint
     if (tid == 0 && total) *total = carry_s;
 }
 
-// One warp per CTA, G atoms per warp (rc_lanes_for): G = 1 runs the scalar
-// decoder on lane 0, G > 1 the lockstep decoder on lanes 0..G-1.
-__global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G) {
+// One warp per CTA, G atoms per warp (rc_lanes_for): G = 1 runs a scalar
+// decoder on lane 0 (the latency decoder when `lat`), G > 1 the lockstep
+// decoder on lanes 0..G-1. With J.order (G = 1 only), CTA i decodes the i-th
+// atom of the payload-length order.
+__global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G, uint32_t lat) {
     __shared__ uint32_t bstart[9];
     if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
     __syncthreads();
     const uint32_t lane = threadIdx.x;
     if (G == 1 && lane != 0) return;
-    const uint64_t t = (uint64_t)blockIdx.x * G + lane;
+    uint64_t t = (uint64_t)blockIdx.x * G + lane;
+    if (J.order) {
+        if (t >= J.sort_ctl[kSortBuckets]) return;
+        t = J.order[t];
+    }
     bool active = false;
     vcd_atom e = {};
     if (lane < G && t < J.n_atoms) {
@@ -120,7 +126,8 @@ __global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G) {
     };
     int bad = 0;
     if (G == 1) {
-        if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
+        if (active && lat) bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1, bstart, sink);
+        else if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
     } else {
         bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart, sink);
     }
@@ -232,21 +239,35 @@ __global__ void __launch_bounds__(kLaneThreads) k_rc_lanes(DecodeJob J) {
     if (L.bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
 }
 
-// The range decode of every PRESENT box atom: above rc_scalar_warps() atoms per
-// SM sub-partition (and with an order buffer) the per-lane decoder over atoms
-// sorted by payload length, else one atom per warp (scalar decoder).
+static void launch_len_sort(const DecodeJob &J, cudaStream_t s) {
+    const unsigned nb = (unsigned)((J.n_atoms + 255) / 256);
+    cudaMemsetAsync(J.sort_ctl, 0, sort_ctl_words() * 4, s);
+    k_len_hist<<<nb, 256, 0, s>>>(J);
+    k_len_scan<<<1, 1024, 0, s>>>(J.sort_ctl);
+    k_len_scatter<<<nb, 256, 0, s>>>(J);
+}
+
+// The range decode of every PRESENT box atom:
+//   up to one atom per SM sub-partition: latency decoder, one atom per warp;
+//   up to rc_scalar_warps() per sub-partition: scalar decoder, one atom per
+//     warp, longest payload first (the tail is the shortest atoms);
+//   above: the per-lane decoder over atoms sorted by payload length.
+// Without an order buffer (no-alloc path) the unsorted forms are used.
 static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s) {
     const uint32_t G = rc_lanes_for(J.n_atoms, (uint32_t)num_sms, rc_scalar_warps());
-    if (G > 1 && J.order && J.sort_ctl) {
-        const unsigned nb = (unsigned)((J.n_atoms + 255) / 256);
-        cudaMemsetAsync(J.sort_ctl, 0, sort_ctl_words() * 4, s);
-        k_len_hist<<<nb, 256, 0, s>>>(J);
-        k_len_scan<<<1, 1024, 0, s>>>(J.sort_ctl);
-        k_len_scatter<<<nb, 256, 0, s>>>(J);
+    const bool sorted = J.order && J.sort_ctl && rc_sorts(J.n_atoms, (uint32_t)num_sms);
+    if (sorted) launch_len_sort(J, s);
+    if (G > 1 && sorted) {
         k_rc_lanes<<<(unsigned)((J.n_atoms + kLaneThreads - 1) / kLaneThreads), kLaneThreads, 0, s>>>(J);
         return;
     }
-    k_rc_decode<<<(unsigned)((J.n_atoms + G - 1) / G), 32, 0, s>>>(J, G);
+    DecodeJob Jr = J;
+    if (!sorted) {
+        Jr.order = nullptr;
+        Jr.sort_ctl = nullptr;
+    }
+    const uint32_t lat = J.n_atoms <= 4ull * (uint64_t)num_sms ? 1u : 0u;
+    k_rc_decode<<<(unsigned)((J.n_atoms + G - 1) / G), 32, 0, s>>>(Jr, G, lat);
 }
 
 __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {

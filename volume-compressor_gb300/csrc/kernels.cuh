@@ -87,15 +87,14 @@ struct BatchShape {              // tunables the autotuner chooses among
 };
 
 // Atoms per warp for the range decoder. A warp that decodes one atom runs the
-// scalar decoder, whose latency per atom is the lowest; a warp of several atoms
-// runs them in lockstep, which costs more decision steps per atom but issues
-// each instruction for all of them. One atom per warp while that makes at most
-// `scalar_warps` warps per SM sub-partition (4 per SM; measured on GB300, the
-// scalar decoder wins up to about 16 per sub-partition). Otherwise the fewest
-// warps per sub-partition k that keep a warp at 32 atoms or fewer, and the
-// atoms spread evenly over k warps per sub-partition: for 32,768 atoms on 152
-// SMs that is 27 atoms in 1,214 warps (at most 2 per sub-partition) rather than
-// 32 in 1,024 (2 on 416 sub-partitions, 1 on the rest), 3 % faster measured.
+// scalar decoder, whose latency per atom is the lowest. One atom per warp while
+// that makes at most `scalar_warps` warps per SM sub-partition (4 per SM);
+// above that the plain decode path runs the per-lane decoder (k_rc_lanes: all
+// 32 lanes of a warp, each its own atom; measured on GB300 it overtakes the
+// scalar decoder between 2,048 and 4,096 atoms, and at 9,728 t10 atoms it
+// takes 5.4 ms against 11.8 ms). The batched path still runs the lockstep
+// decoder for G > 1: the fewest warps per sub-partition k that keep a warp at
+// 32 atoms or fewer, the atoms spread evenly over k warps per sub-partition.
 __host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms, uint32_t scalar_warps) {
     const uint64_t slots = 4ull * sms;
     if (n_atoms <= (uint64_t)scalar_warps * slots) return 1;
@@ -103,7 +102,10 @@ __host__ __device__ inline uint32_t rc_lanes_for(uint64_t n_atoms, uint32_t sms,
     const uint64_t g = (n_atoms + k * slots - 1) / (k * slots);
     return g < 2 ? 2u : (uint32_t)g;
 }
-constexpr uint32_t kRcScalarWarpsDefault = 16;
+constexpr uint32_t kRcScalarWarpsDefault = 8;   // measured crossover with the per-lane decoder: 3-5k atoms
+// the plain decode path puts atoms in payload-length order (and needs the order
+// buffer) above one atom per SM sub-partition
+__host__ __device__ inline bool rc_sorts(uint64_t n_atoms, uint32_t sms) { return n_atoms > 4ull * sms; }
 
 // policy of the plain decode path (vcg_set_rc_scalar_warps)
 uint32_t rc_scalar_warps();

@@ -296,14 +296,22 @@ __device__ __forceinline__ int rc_decode_levels_warp(const uint8_t *src, uint32_
 // one at a time, one byte ahead of the renormalisation that consumes them;
 // bytes past the end read as zero. Probabilities are kept unscaled (12 bits).
 __device__ __forceinline__ uint32_t ld_u8_if(bool on, const uint8_t *ptr, uint32_t old) {
+#ifdef __CUDA_ARCH__
     uint32_t v = old;
     asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.global.nc.u8 %0, [%1];\n\t}"
                  : "+r"(v) : "l"(ptr), "r"((uint32_t)on));
     return v;
+#else
+    return on ? *ptr : old;
+#endif
 }
 __device__ __forceinline__ void st_u32_if(bool on, uint32_t *ptr, uint32_t v) {
+#ifdef __CUDA_ARCH__
     asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u32 [%0], %1;\n\t}"
                  :: "l"(ptr), "r"(v), "r"((uint32_t)on) : "memory");
+#else
+    if (on) *ptr = v;
+#endif
 }
 
 constexpr uint32_t kLaneDone = 15u;
@@ -414,6 +422,109 @@ struct RcLane {
         c = nc;
     }
 };
+
+// ---------------------------------------------------------------- latency decoder
+// One atom on one lane when few atoms share the GPU, so that the dependency
+// chain of one decision is all that counts: both outcomes of a decision (the
+// new range renormalised, the adapted probability) are computed before the
+// compare, which then only selects; the byte fetch is predicated, not
+// branched; and a significance decision takes one branch (a one, or the end of
+// the band). Same results as rc_decode_levels_lane; measured on GB300 with one
+// atom per SM sub-partition 44 ns per decision against 57 ns. With several
+// warps per sub-partition its extra instructions make it slower, so it serves
+// only the latency-bound case.
+struct RcIn {
+    const uint8_t *src;
+    uint32_t pos, len, nxt;   // next byte to fetch (nxt: its value, 0 past the end)
+};
+
+__device__ __forceinline__ uint32_t rc_take_if(bool ren, uint32_t c1, RcIn &in) {
+    const uint32_t nx = in.nxt;
+    const uint32_t np = in.pos + (ren ? 1u : 0u);
+    in.pos = np;
+    in.nxt = ld_u8_if(ren && np < in.len, in.src + np, ren ? 0u : nx);
+    return ren ? (c1 << 8) | nx : c1;
+}
+
+__device__ __forceinline__ bool rc_bit_lat(uint32_t &code, uint32_t &range, uint32_t &p, RcIn &in) {
+    const uint32_t r0 = __umulhi(range, p << 20);
+    const uint32_t p0 = p + ((4096u - p) >> 5), p1 = p - (p >> 5);
+    const uint32_t n1 = range - r0;
+    const bool ren0 = r0 < kTop, ren1 = n1 < kTop;
+    const uint32_t rr0 = ren0 ? r0 << 8 : r0, rr1 = ren1 ? n1 << 8 : n1;
+    const bool b = code >= r0;
+    const uint32_t c1 = b ? code - r0 : code;
+    range = b ? rr1 : rr0;
+    p = b ? p1 : p0;
+    code = rc_take_if(b ? ren1 : ren0, c1, in);
+    return b;
+}
+
+__device__ __forceinline__ bool rc_bypass_lat(uint32_t &code, uint32_t &range, RcIn &in) {
+    const uint32_t r0 = range >> 1;
+    const bool b = code >= r0;
+    const uint32_t c1 = b ? code - r0 : code;
+    const bool ren = r0 < kTop;
+    range = ren ? r0 << 8 : r0;
+    code = rc_take_if(ren, c1, in);
+    return b;
+}
+
+template <class Sink>
+__device__ __forceinline__ int rc_decode_levels_lat(const uint8_t *src, uint32_t len, const uint32_t *band_start,
+                                                    Sink &&sink) {
+    RcIn in;
+    in.src = src;
+    in.len = len;
+    uint32_t code = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < 5; ++i) code = (code << 8) | (i < len ? (uint32_t)__ldg(src + i) : 0u);
+    in.pos = 5;
+    in.nxt = 5 < len ? __ldg(src + 5) : 0u;
+    uint32_t range = 0xFFFFFFFFu, eob = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) eob = (eob << 1) | (rc_bypass_lat(code, range, in) ? 1u : 0u);
+    if (eob > 32768u) eob = 32768u;   // src/vc/vc.c:549
+    uint32_t mag[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) mag[k] = 2048u;
+    for (int bnd = 0; bnd < 8; ++bnd) {
+        uint32_t p = band_start[bnd];
+        if (p >= eob) break;
+        const uint32_t lim = band_start[bnd + 1] < eob ? band_start[bnd + 1] : eob;
+        uint32_t sig = 2048u;
+        for (;;) {
+            const bool one = rc_bit_lat(code, range, sig, in);
+            if (!(one | (p + 1u == lim))) {
+                ++p;
+                continue;
+            }
+            if (one) {
+                uint32_t m = 0;   // unary magnitude, then EG0 escape (src/vc/vc.c:491-506)
+#pragma unroll
+                for (int k = 0; k < 12; ++k) {
+                    if (!rc_bit_lat(code, range, mag[k], in)) {
+                        m = (uint32_t)k + 1u;
+                        break;
+                    }
+                }
+                if (m == 0) {
+                    uint32_t ones = 0;
+                    while (rc_bypass_lat(code, range, in)) {
+                        if (++ones > 32u) return 1;
+                    }
+                    uint32_t x = 1;
+                    for (uint32_t i = 0; i < ones; ++i) x = (x << 1) | (rc_bypass_lat(code, range, in) ? 1u : 0u);
+                    m = 11u + x;
+                }
+                const bool neg = rc_bypass_lat(code, range, in);
+                sink(p, (neg ? 0u - m : m) & 0xFFFFu);
+            }
+            if (++p == lim) break;
+        }
+    }
+    return 0;
+}
 
 // ---------------------------------------------------------------- encoder
 // WRITE = false only tracks the interval width: the byte count of the

@@ -611,7 +611,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     }
     p_err = p_ctl;
     void *p_ord = NULL;   // only large decodes use the per-lane range decoder (launch_rc)
-    if (rc_lanes_for(n, (uint32_t)g_dev.num_sms, rc_scalar_warps()) > 1 &&
+    if (rc_sorts(n, (uint32_t)g_dev.num_sms) &&
         (e = vcd_scratch(c, VCD_BUF_ORD, (n + sort_ctl_words()) * 4 + 16, &p_ord)) != cudaSuccess) {
         vcd_set_error("decode scratch", e);
         return vcd_status_of(e);
