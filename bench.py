@@ -56,6 +56,14 @@ def args_parse():
     return p.parse_args()
 
 
+def golden_named(name):
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            return {c["name"]: c for c in json.load(f)["cases"]}.get(name)
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def golden_case(size, target):
     try:
         with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
@@ -326,6 +334,96 @@ def cpu_decoder(data, threads):
     return "port", run
 
 
+def _pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, int(q * len(v)))] if v else None
+
+
+def cpu_regions(data, reqs, one_n=40, all_n=200, budget_s=8.0, check=None):
+    """Per-request CPU region decode (the oracle's vc_decode_region, a scalar C
+    restatement of the reference's; the reference's own build does not exist on
+    this host) on a bounded sample of the same requests: one host thread in
+    sequence (at most one_n requests or budget_s seconds), then all host threads
+    with that many requests in flight (all_n requests). Latency per request in
+    microseconds; GB/s on box bytes. `check(i, out)` (optional) sees every
+    output of the all-threads pass."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import oraclelib
+    from concurrent.futures import ThreadPoolExecutor
+    o = oraclelib.Archive(data)
+
+    def one(i):
+        lod, box = reqs[i]
+        out = np.empty(_box_bytes(box), np.uint8)
+        t0 = time.perf_counter()
+        s, _ = o.decode_region(lod, box, out)
+        dt = time.perf_counter() - t0
+        assert s == 0
+        if check:
+            check(i, out)
+        return dt
+    lat1, t_end = [], time.perf_counter() + budget_s
+    for i in range(min(one_n, len(reqs))):
+        lat1.append(one(i))
+        if time.perf_counter() > t_end:
+            break
+    n1 = len(lat1)
+    b1 = sum(_box_bytes(reqs[i][1]) for i in range(n1))
+    threads = os.cpu_count() or 1
+    idx = list(range(min(all_n, len(reqs))))
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        latn = list(ex.map(one, idx))
+    wall = time.perf_counter() - t0
+    bn = sum(_box_bytes(reqs[i][1]) for i in idx)
+    o.close()
+    us = lambda v: [x * 1e6 for x in v]   # noqa: E731
+    return {"kind": "port", "cores": threads,
+            "one_thread": {"requests": n1, "p50_us": _pct(us(lat1), 0.5), "p99_us": _pct(us(lat1), 0.99),
+                           "GBps": b1 / max(1e-9, sum(lat1)) / 1e9},
+            "all_cores": {"requests": len(idx), "p50_us": _pct(us(latn), 0.5), "p99_us": _pct(us(latn), 0.99),
+                          "GBps": bn / wall / 1e9},
+            "sample": "the first requests of the same list, oracle vc_decode_region into host memory"}
+
+
+def cpu_encode(vol_slab, q, one_n=256):
+    """CPU encode of the atoms of a host volume slab at base_q q with the oracle's
+    per-atom encoder (forward DCT, quantiser, range coder; the reference's
+    vc_test_atom_rt path, src/vc/vc.c:1582-1590), all host threads over every
+    atom of the slab and one thread over one_n atoms: GB/s of voxels."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import oraclelib
+    from concurrent.futures import ThreadPoolExecutor
+    L = oraclelib.lib()
+    z, y, x = vol_slab.shape
+    atoms = np.ascontiguousarray(vol_slab.reshape(z // 32, 32, y // 32, 32, x // 32, 32)
+                                 .transpose(0, 2, 4, 1, 3, 5).reshape(-1, 32768))
+    threads = os.cpu_count() or 1
+    import threading
+    tl = threading.local()   # one payload buffer per thread
+
+    def enc(i):
+        if not hasattr(tl, "buf"):
+            tl.buf = np.empty(131136, np.uint8)
+        zf, dc = ctypes.c_int(), ctypes.c_uint8()
+        return L.orc_encode_atom(atoms[i].ctypes.data, ctypes.c_float(q), tl.buf.ctypes.data, 131136,
+                                 ctypes.byref(zf), ctypes.byref(dc))
+    t0 = time.perf_counter()
+    for i in range(min(one_n, len(atoms))):
+        enc(i)
+    t1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        total = sum(ex.map(enc, range(len(atoms))))
+    tn = time.perf_counter() - t0
+    return {"kind": "port", "cores": threads, "q": q, "atoms": len(atoms), "coder_bytes": int(total),
+            "all_cores_GBps": len(atoms) * 32768 / tn / 1e9,
+            "one_thread_GBps": min(one_n, len(atoms)) * 32768 / t1 / 1e9,
+            "sample": f"{len(atoms)} atoms of the volume's first {z} planes, fixed q (one encode pass)"}
+
+
 def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
     """BASELINE config 4: 2048x2048x1536 volume at target_ratio 20; n_boxes boxes,
     edges U[32,256] (clamped to the LOD), unaligned offsets, LOD U{0..3}, seed
@@ -366,6 +464,25 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             ms.append(vc.last_call_ms())
     shape = vc.batch_shape()
     batch_ms = min(ms)
+    # the first boxes against the reference's decode of the same archive (golden hashes)
+    import hashlib
+    ref_ok, ref_n = None, 0
+    g = golden_named("cfg4_2048x2048x1536_t20")
+    arc_ok = None if g is None else g["sha256"] == hashlib.sha256(data).hexdigest()
+    if arc_ok:
+        ref_ok = True
+        for i, b in enumerate(g["boxes"]):
+            lod, box = reqs[i]
+            if (lod, list(box)) != (b["lod"], b["box"]):
+                ref_ok = False
+                break
+            nb = (box[3] - box[0]) * (box[4] - box[1]) * (box[5] - box[2])
+            host = np.empty(nb, np.uint8)
+            assert vc.lib().vcg_copy(host.ctypes.data, views[i].ptr, nb) == 0
+            ref_ok = ref_ok and hashlib.sha256(host.tobytes()).hexdigest() == b["sha256"]
+            ref_n += 1
+    elif g:
+        ref_ok = False
     # every candidate of the autotuner on the same batch (forced shape, graph re-captured)
     cand = {}
     L = vc.lib()
@@ -380,6 +497,16 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
                     t.append(vc.last_call_ms())
             cand[f"rc{rcw}_{'imma' if imma else 'butterfly'}{tx}"] = min(t)
     assert L.vcg_set_batch_shape(0, 0, 0) == 0
+    # the CPU's per-request decode of the first boxes, each output compared
+    # with the batch's
+    cpu, cpu_ok = None, [True]
+    if os.environ.get("VC_BENCH_NO_CPU") != "1":
+        def same(i, out):
+            host = np.empty(out.size, np.uint8)
+            assert vc.lib().vcg_copy(host.ctypes.data, views[i].ptr, out.size) == 0
+            cpu_ok[0] = cpu_ok[0] and bool(np.array_equal(host, out))
+        cpu = cpu_regions(data, reqs, one_n=40, all_n=160, check=same)
+        cpu["batch_outputs_equal"] = cpu_ok[0]
     # plain path: one vcg_decode_region_device per request, on a sample
     idx = rng.choice(n_boxes, plain_sample, replace=False)
     plain_ms, plain_bytes = [], 0
@@ -405,7 +532,9 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             "plain_p99_us": plain_ms[min(len(plain_ms) - 1, int(0.99 * len(plain_ms)))] * 1e3,
             "speedup_vs_plain": batch_gbps / plain_gbps, "candidates_ms": cand, "autotuned_shape": {"rc_scalar_warps": shape[0], "transform_imma": shape[2],
                                                                             "transform_threads": shape[1]},
-            "bit_exact_sample": ok, "plain_sample": plain_sample}
+            "bit_exact_sample": ok, "plain_sample": plain_sample,
+            "bit_exact_vs_reference": {"archive": arc_ok, "boxes": ref_ok, "boxes_checked": ref_n},
+            "cpu_baseline": cpu}
 
 
 def _stage_table(stats, peak):
@@ -422,11 +551,15 @@ def config2_sweep(dvol, dims, peak, targets=(10.0, 50.0, 100.0)):
     LOD of each archive decoded into device memory: device time, GB/s and
     per-stage algorithmic GB/s with the fraction of the measured HBM peak;
     archives and decoded LODs are checked against the reference's SHA-256
-    fixtures where they exist."""
+    fixtures where they exist. Beside the encode, the CPU's fixed-q encode of a
+    bounded sample of the same volume."""
     import hashlib
+    import numpy as np
     import vc_gb300 as vc
     nx, ny, nz = dims
     res = {}
+    slab = None if os.environ.get("VC_BENCH_NO_CPU") == "1" else \
+        vc.synth(nx, ny, nz, vc.config_seed(CONFIG_ID), threads=os.cpu_count() or 1, z0=0, z1=min(nz, 128))
     for t in targets:
         vc.profile_enable(True)
         vc.profile_read(reset=True)
@@ -441,6 +574,14 @@ def config2_sweep(dvol, dims, peak, targets=(10.0, 50.0, 100.0)):
                "archive_sha_matches_reference": (hashlib.sha256(data).hexdigest() == g["sha256"]) if g else None}
         s, _, _ = vc.encode_device(dvol, dims, t)   # unprofiled timing
         row["encode_GBps"] = nx * ny * nz / (vc.last_call_ms() / 1e3) / 1e9
+        qs, qq = [], np.float32(q0)
+        for _ in range(8):
+            qs.append(float(max(qq, np.float32(0.05))))
+            qq = np.float32(qq * np.float32(0.6))
+        s, _ = vc.encode_q(dvol, t, qs, on_device=dims)
+        row["encode_fixed_q_GBps"] = nx * ny * nz / (vc.last_call_ms() / 1e3) / 1e9
+        if slab is not None:
+            row["cpu_encode_fixed_q"] = cpu_encode(slab, q0)
         a = vc.Archive(data)
         assert a.make_resident() == 0
         lods, lod_ok = [], []
@@ -877,7 +1018,7 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
     as many host threads as the server has workers). Outputs are host memory;
     large-box outputs rotate through a pool in the timed streams, and a separate
     stream of verify_n requests with distinct outputs is checked byte for byte
-    against vc_decode_region."""
+    against the CPU's decode of each request (the CPU baseline's sample)."""
     import numpy as np
     import vc_gb300 as vc
     n = 2048
@@ -887,7 +1028,7 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
     dv.free()
     a = vc.Archive(data)
     assert a.make_resident() == 0
-    cfg = {"device_budget": 2 << 30, "max_batch": 1024, "workers": 2}
+    cfg = {"device_budget": 2 << 30, "max_batch": 1024, "workers": 3}
     rng = np.random.default_rng(0x5E5E)
     warm = served_mix(a, rng, 64)   # first batches tune the launch shape and build graphs
     wo = [np.empty(_box_bytes(b), np.uint8) for _, b in warm]
@@ -912,8 +1053,14 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
                          ("plain", lambda: _plain_stream(a, reqs, arrivals, outs, cfg["workers"]))):
             r = fn()
             lat, wall = r[0], r[1]
+            lat_a = np.asarray(lat)
+            big = np.array([_box_bytes(b) >= (32 << 20) for _, b in reqs])
             row[name] = {"p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
-                         "GBps": total / wall / 1e9, "achieved_rps": m / wall}
+                         "GBps": total / wall / 1e9, "achieved_rps": m / wall,
+                         "small": {"p50_us": float(np.percentile(lat_a[~big], 50)),
+                                   "p99_us": float(np.percentile(lat_a[~big], 99))} if (~big).any() else None,
+                         "large_512": {"p50_us": float(np.percentile(lat_a[big], 50)),
+                                       "p99_us": float(np.percentile(lat_a[big], 99))} if big.any() else None}
             if name == "server":
                 row[name]["mean_batch"] = r[2]
         sweep.append(row)
@@ -922,21 +1069,21 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
     arrivals = np.cumsum(rng.exponential(1.0 / rates[-1], verify_n))
     outs = [np.empty(_box_bytes(b), np.uint8) for _, b in reqs]
     _serve_stream(a, reqs, arrivals, outs, cfg)
-    ok, ref_cache = True, {}
-    for (lod, box), o in zip(reqs, outs):
-        key = (lod, box)
-        if key not in ref_cache:
-            ref = np.empty(_box_bytes(box), np.uint8)
-            assert a.decode_region(lod, box, ref)[0] == 0
-            ref_cache[key] = ref if _box_bytes(box) == 512 ** 3 else None
-        else:
-            ref = ref_cache[key]
-        ok = ok and bool(np.array_equal(o, ref))
     a.close()
+    # every served output against the CPU's decode of the same request (the
+    # CPU baseline's all-threads pass); one thread on the first requests
+    ok = [True]
+
+    def same(i, out):
+        ok[0] = ok[0] and bool(np.array_equal(outs[i], out))
+    cpu = None
+    if os.environ.get("VC_BENCH_NO_CPU") != "1":
+        cpu = cpu_regions(data, reqs, one_n=60, all_n=verify_n, budget_s=10.0, check=same)
+    ok = ok[0] if cpu else None
     return {"workload": "2048^3 at target_ratio 20 resident in HBM; Poisson arrivals; 70% 32^3 atoms LOD0, "
                         "25% boxes U[64,128]^3 LOD0-1, 5% 512^3 LOD2; host outputs",
             "q0": q0, "archive_bytes": len(data), "server": cfg, "plain_threads": cfg["workers"],
-            "sweep": sweep, "bit_exact_all_outputs": ok, "verified_requests": verify_n}
+            "sweep": sweep, "bit_exact_all_outputs_vs_cpu": ok, "verified_requests": verify_n, "cpu_baseline": cpu}
 
 
 # ---------------------------------------------------------------- arms
@@ -1062,7 +1209,7 @@ def gb300_arm(args, dist):
 
     # per-request region latency (plain path, host output)
     rng = np.random.default_rng(0xB0C5)
-    lat = []
+    lat, region_reqs = [], []
     for _ in range(args.regions):
         lod = int(rng.integers(0, 4))
         dd = arc.lod_dims(lod)[1]
@@ -1073,7 +1220,11 @@ def gb300_arm(args, dist):
         st, _ = arc.decode_region(lod, box)
         lat.append((time.perf_counter() - t0) * 1e6)
         assert st == 0
+        region_reqs.append((lod, box))
     lat.sort()
+    region_cpu = None
+    if dist.rank == 0 and os.environ.get("VC_BENCH_NO_CPU") != "1":
+        region_cpu = cpu_regions(data, region_reqs, one_n=30, all_n=len(region_reqs))
 
     # roofline of the dominant stage
     peak, peak_kind = measured_peak()
@@ -1156,6 +1307,8 @@ def gb300_arm(args, dist):
                             (v["bytes_read"] + v["bytes_written"]) / max(1e-9, v["ms"] / 1e3) / 1e9}
                         for k, v in stats.items()}
     detail["encode_GBps"] = nbytes / (statistics.median(enc_ms) / 1e3) / 1e9
+    if region_cpu:
+        detail["region_latency_cpu"] = region_cpu
     detail["encode_with_rate_control_GBps"] = nbytes / (enc_full_ms / 1e3) / 1e9
     if cpu:
         detail["cpu_baseline"] = cpu

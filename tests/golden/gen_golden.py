@@ -10,6 +10,8 @@ reference's own tests use (tests/test_vc.c, tests/test_coverage.c).
 Output: tests/golden/golden.json (+ small archives as *.vca.xz).
     python tests/golden/gen_golden.py            # standard set (~1 min)
     python tests/golden/gen_golden.py --big      # + 1024^3 config at targets 10/50/100 (~15 min)
+    python tests/golden/gen_golden.py --cfg4 --append   # + the 2048x2048x1536 t20 archive
+                                                        #   and its first region boxes (~30 min)
 """
 import hashlib
 import json
@@ -146,6 +148,44 @@ def writer_case(name, dims, vol, q, skip=(), zero_marks=()):
             "skip": [list(s) for s in skip], "zero_marks": [list(z) for z in zero_marks]}
 
 
+def config4_boxes(dims, nlod, n, seed=0xB0C5):
+    """The batched-decode box list of the 2048x2048x1536 workload: LOD U{0..3},
+    edges U[32,256] clamped to the LOD, offsets U[0, dim - edge] (numpy
+    default_rng; bench.py draws the same sequence)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        lod = int(rng.integers(0, 4))
+        d = R.lod_dims(*dims, lod)
+        e = [int(min(rng.integers(32, 257), d[k])) for k in range(3)]
+        o = [int(rng.integers(0, d[k] - e[k] + 1)) for k in range(3)]
+        out.append((lod, (o[0], o[1], o[2], o[0] + e[0], o[1] + e[1], o[2] + e[2])))
+    return out
+
+
+def config4_case(n_boxes=400):
+    """2048x2048x1536 at target_ratio 20 (the batched / served workload): the
+    archive's hash and the reference's decode of the first n_boxes boxes."""
+    dims = (2048, 2048, 1536)
+    seed = V.config_seed(4)
+    vol = V.synth(*dims, seed, threads=os.cpu_count())
+    data, q0 = R.ref_encode(vol, 20.0, threads=os.cpu_count())
+    vsha = sha(vol)
+    del vol
+    nlod = R.nlod_of(*dims)
+    a = R.RefArchive(data)
+    boxes = []
+    for lod, box in config4_boxes(dims, nlod, n_boxes):
+        s, out = a.decode_region(lod, box)
+        assert s == 0
+        boxes.append({"lod": lod, "box": list(box), "sha256": sha(out)})
+    a.close()
+    print(f"cfg4: q0={q0} len={len(data)}", flush=True)
+    return {"name": "cfg4_2048x2048x1536_t20", "kind": "synth", "dims": list(dims), "seed": seed, "target": 20.0,
+            "q0": q0, "nlod": nlod, "len": len(data), "sha256": sha(data), "volume_sha256": vsha,
+            "box_seed": 0xB0C5, "boxes": boxes}
+
+
 def main():
     big = "--big" in sys.argv
     cases = json.load(open(OUT))["cases"] if os.path.exists(OUT) and "--append" in sys.argv else []
@@ -154,7 +194,9 @@ def main():
     def add(c):
         cases[:] = [x for x in cases if x["name"] != c["name"]] + [c]
 
-    if not big or "cfg1_256_t10" not in names:
+    if "--cfg4" in sys.argv:
+        add(config4_case())
+    elif not big or "cfg1_256_t10" not in names:
         add(synth_case("cfg1_256_t10", (256, 256, 256), V.config_seed(1), 10.0, keep=False, nboxes=10))
         add(synth_case("synth_64_t10", (64, 64, 64), 0x5EED1001, 10.0))
         add(synth_case("synth_prime_97x131x65_t20", (97, 131, 65), 0x5EED1002, 20.0))

@@ -1,6 +1,8 @@
-"""Batched region decode (vcg_decode_regions): every request equals the plain
-vc_decode_region result (status and bytes), for host and device outputs,
-across graph replays, buffer growth and a corrupt archive."""
+"""Batched region decode (vcg_decode_regions): every request equals what the
+oracle's vc_decode_region gives for it alone (status and bytes, including the
+partial output of a request stopped by a malformed atom), for host and device
+outputs, across graph replays, buffer growth, every launch shape and a corrupt
+archive."""
 import struct
 
 import numpy as np
@@ -29,7 +31,16 @@ def box_bytes(box):
     return max(0, (x1 - x0) * (y1 - y0) * (z1 - z0))
 
 
+def oracle_of(a):
+    """The oracle's handle on the same archive bytes as the product's handle a."""
+    import oraclelib
+    if getattr(a, "_oracle", None) is None:
+        a._oracle = oraclelib.Archive(bytes(a.buf.raw))
+    return a._oracle
+
+
 def check(vc, a, reqs, on_device):
+    o = oracle_of(a)
     if on_device:
         outs = [vc.DeviceBuffer(max(1, box_bytes(b))) for _, b in reqs]
     else:
@@ -38,7 +49,7 @@ def check(vc, a, reqs, on_device):
     assert s == vc.VC_OK
     for i, (lod, box) in enumerate(reqs):
         ref = np.full(max(1, box_bytes(box)), 0x5A, np.uint8)
-        s2, _ = a.decode_region(lod, box, ref)
+        s2, _ = o.decode_region(lod, box, ref)
         assert st[i] == s2, (i, lod, box)
         got = outs[i].download(max(1, box_bytes(box))) if on_device else outs[i]
         if s2 == vc.VC_OK:
@@ -46,7 +57,7 @@ def check(vc, a, reqs, on_device):
 
 
 @pytest.mark.parametrize("name", ["synth_prime_97x131x65_t20", "ref_test_basic", "synth_64_t10"])
-def test_batch_matches_plain_host_and_device(vc, gpu, golden, name):
+def test_batch_matches_oracle_host_and_device(vc, gpu, golden, name):
     a = vc.Archive(load_archive(golden[name]))
     rng = np.random.default_rng(11)
     nlod = struct.unpack_from("<I", load_archive(golden[name]), 20)[0]
@@ -63,7 +74,7 @@ def test_batch_graph_replay_and_growth(vc, gpu, golden):
         check(vc, a, random_requests(a, rng, n, 2, max_edge=edge), on_device=True)
 
 
-def test_batch_on_corrupt_archive_matches_plain(vc, gpu, golden):
+def test_batch_on_corrupt_archive_matches_oracle(vc, gpu, golden):
     from test_gpu_decode import _slot_offset
     data = bytearray(load_archive(golden["synth_prime_97x131x65_t20"]))
     so = _slot_offset(data, 0, 1, 2, 1)   # break the payload range of LOD0 atom (1, 2, 1)
@@ -77,9 +88,9 @@ def test_batch_on_corrupt_archive_matches_plain(vc, gpu, golden):
 
 @pytest.mark.parametrize("shape", [(1, 256, 0), (4, 256, 0), (16, 256, 0), (1, 512, 0), (4, 512, 0), (16, 512, 0),
                                    (1, 256, 1), (4, 256, 1), (16, 256, 1)])
-def test_every_launch_shape_matches_plain(vc, gpu, golden, shape):
+def test_every_launch_shape_matches_oracle(vc, gpu, golden, shape):
     """Each candidate of the autotuner (range-decoder policy x transform size x
-    butterfly / int8 tensor-core transform) gives the plain decode's bytes and
+    butterfly / int8 tensor-core transform) gives the oracle's bytes and
     statuses, also on a corrupt archive."""
     from test_gpu_decode import _slot_offset
     L = vc.lib()
@@ -121,5 +132,25 @@ def test_many_boxes_over_one_atom(vc, gpu, golden, shape):
             reqs.append((0, (x0, y0, z0, x1, y1, z1)))
         check(vc, a, reqs, on_device=True)
         check(vc, a, reqs, on_device=False)
+    finally:
+        assert L.vcg_set_batch_shape(0, 0, 0) == 0
+
+
+def test_batch_lane_decoder_matches_oracle(vc, gpu):
+    """A batch with more distinct atoms than one per warp (range-decoder policy
+    1: above 4 x SMs atoms) goes to the per-lane decoder in payload-length
+    order; every request equals the oracle's decode of it alone."""
+    n = 512
+    dv = vc.synth_device(n, n, n, vc.config_seed(2))
+    s, data = vc.encode_q(dv, 20.0, [2.6 * 0.6 ** l for l in range(8)], on_device=(n, n, n))
+    assert s == 0
+    dv.free()
+    a = vc.Archive(data)
+    L = vc.lib()
+    assert L.vcg_set_batch_shape(1, 512, 0) == 0
+    try:
+        rng = np.random.default_rng(16)
+        reqs = random_requests(a, rng, 400, 0, max_edge=70)
+        check(vc, a, reqs, on_device=True)
     finally:
         assert L.vcg_set_batch_shape(0, 0, 0) == 0

@@ -1,7 +1,8 @@
 """Decode server (vcg_server_*): requests submitted from several host threads
 into the continuous-batching loop come back with exactly the status and bytes
-vc_decode_region gives for that request alone, under a device-memory budget
-that forces admission to wait, with batches of several workers in flight."""
+the oracle's vc_decode_region gives for that request alone, under a
+device-memory budget that forces admission to wait, with batches of several
+workers in flight."""
 import struct
 import threading
 
@@ -9,7 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import load_archive
-from test_gpu_batch import box_bytes, random_requests
+from test_gpu_batch import box_bytes, oracle_of, random_requests
 
 
 def run_mixed(vc, a, reqs, threads, budget, max_batch, workers):
@@ -33,9 +34,10 @@ def run_mixed(vc, a, reqs, threads, budget, max_batch, workers):
 
 
 def check_alone(vc, a, reqs, outs, res):
+    o = oracle_of(a)
     for i, (lod, box) in enumerate(reqs):
         ref = np.full(max(1, box_bytes(box)), 0x5A, np.uint8)
-        s, _ = a.decode_region(lod, box, ref)
+        s, _ = o.decode_region(lod, box, ref)
         assert res[i][0] == s, (i, lod, box)
         assert res[i][1] >= 0.0
         if s == vc.VC_OK:
@@ -81,9 +83,10 @@ def test_server_destroy_drains_queue(vc, gpu, golden):
     for (lod, box), o in zip(reqs, outs):
         assert srv.submit(lod, box, o) >= 0
     srv.close()   # returns only after every queued request ran
+    ora = oracle_of(a)
     for (lod, box), o in zip(reqs, outs):
         ref = np.zeros(max(1, box_bytes(box)), np.uint8)
-        s, _ = a.decode_region(lod, box, ref)
+        s, _ = ora.decode_region(lod, box, ref)
         assert s == vc.VC_OK and np.array_equal(o, ref)
 
 

@@ -17,8 +17,9 @@ namespace vcg {
 constexpr size_t kTileSmem = kTileBytes;   // the butterfly's padded tile (idct_tile.cuh)
 
 // Persistent over the batch's distinct atoms (their number is read from device
-// memory): G atoms per warp by rc_lanes_for, scalar decoder for G = 1, lockstep
-// decoder otherwise.
+// memory) while the policy keeps one atom per warp (rc_lanes_for gives 1):
+// scalar decoder. With more atoms, k_rc_batch_lanes takes them instead (or,
+// without its order buffer, the lockstep decoder here).
 constexpr int kRcBatchThreads = 128;
 
 __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
@@ -27,6 +28,7 @@ __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
     __syncthreads();
     const uint32_t n = *J.n_ua;
     const uint32_t G = rc_lanes_for(n, J.sms, J.rc_scalar_warps);
+    if (G > 1 && J.order) return;   // k_rc_batch_lanes decodes this batch
     const uint32_t lane = threadIdx.x & 31u;
     if (G == 1 && lane != 0) return;
     const uint64_t nwarps = (uint64_t)gridDim.x * (kRcBatchThreads / 32);
@@ -52,7 +54,9 @@ __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
         };
         int bad = 0;
         if (G == 1) {
-            if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
+            // up to one atom per SM sub-partition the latency decoder, else the compact scalar one
+            if (active && n <= 4u * J.sms) bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1, bstart, sink);
+            else if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
         } else {
             bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart, sink);
         }
@@ -62,6 +66,71 @@ __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
             const UAtom a = J.ua[u];
             for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) atomicOr(J.req_err + J.dst[d], 1u);
         }
+    }
+}
+
+// ---- per-lane decoder over the distinct atoms, in payload-length order
+// (the same counting sort as the plain path's), when the policy gives more
+// than one atom per warp. The counts are read from device memory, so these
+// run in the batch's graph; with one atom per warp they return at once.
+__device__ __forceinline__ uint32_t ua_bucket(uint32_t len) {
+    const uint32_t k = len >> 5;
+    return kSortBuckets - 1u - (k < kSortBuckets - 1u ? k : kSortBuckets - 1u);
+}
+
+__global__ void k_ua_hist(BatchJob J) {
+    const uint32_t n = *J.n_ua;
+    if (rc_lanes_for(n, J.sms, J.rc_scalar_warps) == 1) return;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+        const vcd_atom e = J.atoms[J.ua[u].idx];
+        if (e.kind == VCD_PRESENT) atomicAdd(&J.sort_ctl[ua_bucket(e.len)], 1u);
+        else J.cnt[u] = 0;
+    }
+}
+
+__global__ void k_ua_scatter(BatchJob J) {
+    const uint32_t n = *J.n_ua;
+    if (rc_lanes_for(n, J.sms, J.rc_scalar_warps) == 1) return;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+        const vcd_atom e = J.atoms[J.ua[u].idx];
+        if (e.kind == VCD_PRESENT) J.order[atomicAdd(&J.sort_ctl[ua_bucket(e.len)], 1u)] = u;
+    }
+}
+
+constexpr int kBatchLaneThreads = 64;
+
+__global__ void __launch_bounds__(kBatchLaneThreads) k_rc_batch_lanes(BatchJob J) {
+    __shared__ uint32_t bstart[9];
+    __shared__ uint32_t S[12 * kBatchLaneThreads];
+    if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
+    __syncthreads();
+    const uint32_t n_present = J.sort_ctl[kSortBuckets];   // 0 when the scalar kernel decodes this batch
+    if ((uint64_t)blockIdx.x * kBatchLaneThreads >= n_present) return;   // whole CTA idle
+    const uint32_t i = blockIdx.x * kBatchLaneThreads + threadIdx.x;
+    const bool active = i < n_present;
+    uint32_t u = 0, cap = 0;
+    vcd_atom e = {};
+    uint32_t *dst = J.ent;
+    if (active) {
+        u = J.order[i];
+        e = J.atoms[J.ua[u].idx];
+        cap = 8u * (e.len - 1u) + 64u;
+        if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+        dst = J.ent + J.ent_off[u];
+    }
+    uint32_t *Sl = S + threadIdx.x;
+    RcLane L;
+    L.init(J.arc + e.off + 1, e.len - 1u, active, bstart, Sl, kBatchLaneThreads, dst, cap);
+    while (__any_sync(0xFFFFFFFFu, L.c != kLaneDone)) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) L.step(bstart, Sl, kBatchLaneThreads);
+    }
+    if (!active) return;
+    const uint32_t cnt = L.n > cap ? cap : L.n;
+    J.cnt[u] = cnt | (L.n > cap ? kEntOverflow : 0u) | (L.bad ? kEntBad : 0u);
+    if (L.bad) {
+        const UAtom a = J.ua[u];
+        for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) atomicOr(J.req_err + J.dst[d], 1u);
     }
 }
 
@@ -302,6 +371,16 @@ static void launch_rc(const BatchJob &J, int num_sms, uint32_t max_ua, cudaStrea
     if (warps > cap) warps = cap;
     if (warps < 1) warps = 1;
     const unsigned grid = (unsigned)((warps * 32 + kRcBatchThreads - 1) / kRcBatchThreads);
+    if (J.order && J.sort_ctl) {   // the per-lane decoder's launches (idle when one atom per warp)
+        const uint64_t sort_grid = ((uint64_t)max_ua + 255) / 256;
+        const unsigned sg = (unsigned)(sort_grid < 1 ? 1 : sort_grid > 4096 ? 4096 : sort_grid);
+        cudaMemsetAsync(J.sort_ctl, 0, sort_ctl_words() * 4, s);
+        k_ua_hist<<<sg, 256, 0, s>>>(J);
+        launch_len_scan(J.sort_ctl, s);
+        k_ua_scatter<<<sg, 256, 0, s>>>(J);
+        const uint64_t lg = ((uint64_t)max_ua + kBatchLaneThreads - 1) / kBatchLaneThreads;
+        k_rc_batch_lanes<<<(unsigned)(lg < 1 ? 1 : lg), kBatchLaneThreads, 0, s>>>(J);
+    }
     k_rc_batch<<<grid, kRcBatchThreads, 0, s>>>(J);
 }
 

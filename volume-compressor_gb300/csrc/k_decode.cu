@@ -239,6 +239,8 @@ __global__ void __launch_bounds__(kLaneThreads) k_rc_lanes(DecodeJob J) {
     if (L.bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
 }
 
+void launch_len_scan(uint32_t *sort_ctl, cudaStream_t s) { k_len_scan<<<1, 1024, 0, s>>>(sort_ctl); }
+
 static void launch_len_sort(const DecodeJob &J, cudaStream_t s) {
     const unsigned nb = (unsigned)((J.n_atoms + 255) / 256);
     cudaMemsetAsync(J.sort_ctl, 0, sort_ctl_words() * 4, s);

@@ -79,6 +79,8 @@ struct BatchJob {
     uint32_t band_start[9];
     uint32_t sms;                // SM count of the device
     uint32_t rc_scalar_warps;    // range-decoder policy (rc_lanes_for)
+    uint32_t *order;             // distinct atoms in payload-length order (per-lane decoder)
+    uint32_t *sort_ctl;          // kSortBuckets counters + present-atom count
 };
 struct BatchShape {              // tunables the autotuner chooses among
     int rc_scalar_warps;         // range-decoder policy: 1, 4 or 16 (rc_lanes_for)
@@ -122,6 +124,8 @@ void launch_idct(const DecodeJob &J, int num_sms, cudaStream_t s, uint64_t t_lo,
 // atom's list offset (each list can take VCD_MAX_ENTRIES entries).
 void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s);
 void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cudaStream_t s);
+// exclusive scan of the kSortBuckets length counters in place, their sum after them
+void launch_len_scan(uint32_t *sort_ctl, cudaStream_t s);
 
 // cudaFuncAttributeMaxDynamicSharedMemorySize of kernel fn, set on the calling
 // thread's current device. The attribute belongs to the device's context, not

@@ -141,6 +141,10 @@ extern "C" int vcd_decode_batch(vcd_archive *d, const vcd_batch *b, uint8_t *con
     memcpy(J.band_start, g_dev.band_start, sizeof J.band_start);
     // capacity in distinct atoms the range-decode grid must cover (the buffer's)
     const uint32_t max_ua = (uint32_t)((cap_of(c, VCD_BUF_BUA) - 64) / sizeof(vcd_uatom));
+    void *p_ord;
+    CKB(vcd_scratch(c, VCD_BUF_BORD, ((size_t)max_ua + sort_ctl_words()) * 4 + 64, &p_ord), "batch order");
+    J.sort_ctl = (uint32_t *)p_ord;
+    J.order = J.sort_ctl + sort_ctl_words();
 
     const int forced = __atomic_load_n(&g_forced_shape, __ATOMIC_ACQUIRE);
     if (forced) {

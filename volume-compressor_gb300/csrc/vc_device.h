@@ -14,6 +14,7 @@ enum {
     VCD_BUF_BPIN, VCD_BUF_COEF, VCD_BUF_RPK, VCD_BUF_RPKREC, VCD_BUF_STG, VCD_BUF_WPACK,
     VCD_BUF_EENT2, VCD_BUF_EMETA2,   // encode: lists and metadata of the coarser LODs (second stream)
     VCD_BUF_ORD,                     // decode: atom order of the per-lane range decoder + sort counters
+    VCD_BUF_BORD,                    // batched decode: the same for the distinct atoms
     VCD_NBUF
 };
 

@@ -2,14 +2,19 @@
 // archive kept resident in device memory.
 //
 // Requests are queued by vcg_server_submit and decoded by a small pool of
-// worker threads, each with its own CUDA stream. A worker takes, in arrival
-// order, as many waiting requests as the shared device-memory budget and its
-// batch limit allow, decodes them in one batched pass (each distinct atom once,
-// cropped into every box; vcg_decode_regions) and releases their budget.
-// Requests that arrive while batches are on the GPU join the next batch of
-// whichever worker frees up first, so batches from different workers overlap on
-// the device. Each result is exactly what vc_decode_region returns for that
-// request alone.
+// worker threads, each with its own CUDA stream. Requests fall in two classes
+// by box size. A worker takes, in arrival order, as many waiting small
+// requests as the shared device-memory budget and its batch limit allow,
+// decodes them in one batched pass (each distinct atom once, cropped into
+// every box; vcg_decode_regions) and releases their budget; a batch of one
+// request takes the plain decode path (vc_decode_region), which has the lower
+// latency. A large request (kBigVoxels or more) runs alone through the plain
+// path when it is the oldest request waiting, on at most workers - 1 workers at
+// a time, so that one worker always serves the small requests and a small
+// request never waits behind a large one's decode. Requests that arrive while
+// batches are on the GPU join the next batch of whichever worker frees up
+// first, so batches from different workers overlap on the device. Each result
+// is exactly what vc_decode_region returns for that request alone.
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -20,9 +25,12 @@
 #define VC_API __attribute__((visibility("default")))
 
 
+#define kBigVoxels (32ull << 20)   // a box of 32 Mi voxels or more is a large request
+
 typedef struct {
     vcg_region_request req;
     uint64_t cost;          // device bytes the request holds while decoding
+    int big;                // box of kBigVoxels or more
     double t_submit, t_done;
     vc_status status;
     int state;              // 0 queued, 1 running, 2 done, 3 done and waited for
@@ -40,6 +48,8 @@ typedef struct vcg_server {
     uint64_t cap, base, n;  // slots, ticket of reqs[0], tickets issued
     uint64_t head;          // first ticket not yet taken by a worker
     uint64_t lo;            // every ticket below lo has been waited for
+    uint64_t q_small, q_big;   // queued (not yet taken) requests of each class
+    int big_running;        // workers decoding a large request
     uint64_t batches, batched_reqs;
 } vcg_server;
 
@@ -65,31 +75,64 @@ static void *worker(void *arg) {
     vcg_region_request *batch = (vcg_region_request *)malloc(s->max_batch * sizeof(vcg_region_request));
     vc_status *st = (vc_status *)malloc(s->max_batch * sizeof(vc_status));
     uint64_t *tix = (uint64_t *)malloc(s->max_batch * sizeof(uint64_t));
+    const int big_slots = s->nworkers > 1 ? s->nworkers - 1 : 1;
     pthread_mutex_lock(&s->mu);
     for (;;) {
-        while (!s->stop && s->head == s->n) pthread_cond_wait(&s->work_cv, &s->mu);
-        if (s->stop && s->head == s->n) break;
-        // admit in arrival order while memory and the batch limit allow; a
-        // request larger than the whole budget runs alone
+        while (!s->stop && s->q_small + s->q_big == 0) pthread_cond_wait(&s->work_cv, &s->mu);
+        if (s->stop && s->q_small + s->q_big == 0) break;
+        // the oldest waiting request decides: a large one runs alone if a
+        // large-request slot is free; else the small requests in arrival order,
+        // while memory and the batch limit allow. A request larger than the
+        // whole budget runs alone.
         uint32_t k = 0;
         uint64_t take = 0;
-        while (s->head < s->n && k < s->max_batch) {
-            srv_req *r = slot(s, s->head);
-            if (s->in_use + take + r->cost > s->budget && (k > 0 || s->in_use > 0)) break;
-            r->state = 1;
-            batch[k] = r->req;
-            tix[k] = s->head;
-            take += r->cost;
-            ++k;
-            ++s->head;
+        int big = 0;
+        while (s->head < s->n && slot(s, s->head)->state != 0) ++s->head;
+        const int oldest_big = s->head < s->n && slot(s, s->head)->big;
+        if (s->q_small && !(oldest_big && s->big_running < big_slots)) {
+            for (uint64_t t = s->head; t < s->n && k < s->max_batch; ++t) {
+                srv_req *r = slot(s, t);
+                if (r->state != 0 || r->big) continue;
+                if (s->in_use + take + r->cost > s->budget && (k > 0 || s->in_use > 0)) break;
+                r->state = 1;
+                batch[k] = r->req;
+                tix[k] = t;
+                take += r->cost;
+                ++k;
+            }
+            s->q_small -= k;
+        } else if (s->q_big && s->big_running < big_slots) {
+            for (uint64_t t = s->head; t < s->n; ++t) {
+                srv_req *r = slot(s, t);
+                if (r->state != 0) continue;
+                if (s->in_use + r->cost <= s->budget || s->in_use == 0) {
+                    r->state = 1;
+                    batch[0] = r->req;
+                    tix[0] = t;
+                    take = r->cost;
+                    k = 1;
+                    big = 1;
+                    s->q_big -= 1;
+                    s->big_running += 1;
+                }
+                break;
+            }
         }
-        if (k == 0) {   // waiting for memory held by other workers
-            pthread_cond_wait(&s->done_cv, &s->mu);
+        while (s->head < s->n && slot(s, s->head)->state != 0) ++s->head;
+        if (k == 0) {   // waiting for memory or a large-request slot held by other workers
+            pthread_cond_wait(&s->work_cv, &s->mu);
             continue;
         }
         s->in_use += take;
         pthread_mutex_unlock(&s->mu);
-        vc_status rc = vcg_decode_regions(s->a, k, batch, 0, st);
+        vc_status rc;
+        if (k == 1) {   // alone: the plain path
+            rc = vc_decode_region(s->a, batch[0].lod, batch[0].box, batch[0].out);
+            st[0] = rc;
+            rc = rc == VC_ERR_RANGE || rc == VC_ERR_FORMAT ? VC_OK : rc;   // per-request statuses
+        } else {
+            rc = vcg_decode_regions(s->a, k, batch, 0, st);
+        }
         double t = now_us();
         pthread_mutex_lock(&s->mu);
         for (uint32_t i = 0; i < k; ++i) {
@@ -99,6 +142,7 @@ static void *worker(void *arg) {
             r->state = 2;
         }
         s->in_use -= take;
+        s->big_running -= big;
         s->batches++;
         s->batched_reqs += k;
         pthread_cond_broadcast(&s->done_cv);
@@ -156,10 +200,14 @@ VC_API int64_t vcg_server_submit(vcg_server *s, int lod, vc_box box, uint8_t *ou
     r->req.lod = lod;
     r->req.box = box;
     r->req.out = out;
-    r->cost = box.x1 > box.x0 && box.y1 > box.y0 && box.z1 > box.z0 ? cost_of(&box) : 0;
+    const int nonempty = box.x1 > box.x0 && box.y1 > box.y0 && box.z1 > box.z0;
+    r->cost = nonempty ? cost_of(&box) : 0;
+    r->big = nonempty && (uint64_t)(box.x1 - box.x0) * (box.y1 - box.y0) * (box.z1 - box.z0) >= kBigVoxels;
+    if (r->big) s->q_big++;
+    else s->q_small++;
     r->t_submit = now_us();
     int64_t ticket = (int64_t)s->n++;
-    pthread_cond_signal(&s->work_cv);
+    pthread_cond_broadcast(&s->work_cv);
     pthread_mutex_unlock(&s->mu);
     return ticket;
 }
