@@ -194,6 +194,8 @@ class Clocks:
 # What bounds each decode stage, from the ncu captures of this workload (an HBM
 # fraction alone misreads a latency-bound kernel).
 LIMITER = {
+    "decode_fused": "the range decoders' dependency chains (8 warps per SM) beside the transform's integer multiplies "
+                    "(8 warps per SM) in one kernel",
     "rc_decode": "dependency chain of each serial range decoder: 44 % issue active, DRAM under 1 % busy (ncu)",
     "idct": "integer pipes of the inverse passes: 52 % issue active, DRAM 6 % busy (ncu)",
 }
@@ -1228,7 +1230,7 @@ def gb300_arm(args, dist):
 
     # roofline of the dominant stage
     peak, peak_kind = measured_peak()
-    dom = max((k for k in stats if k in ("idct", "rc_decode")), key=lambda k: stats[k]["ms"])
+    dom = max((k for k in stats if k in ("idct", "rc_decode", "decode_fused")), key=lambda k: stats[k]["ms"])
     st_ = stats[dom]
     per_launch_bytes = (st_["bytes_read"] + st_["bytes_written"]) / max(1, st_["launches"])
     per_launch_ms = st_["ms"] / max(1, st_["launches"])

@@ -12,6 +12,8 @@ Output: tests/golden/golden.json (+ small archives as *.vca.xz).
     python tests/golden/gen_golden.py --big      # + 1024^3 config at targets 10/50/100 (~15 min)
     python tests/golden/gen_golden.py --cfg4 --append   # + the 2048x2048x1536 t20 archive
                                                         #   and its first region boxes (~30 min)
+    python tests/golden/gen_golden.py --cfg5 --append   # + the 2048^3 t20 archive and a
+                                                        #   served request mix (~40 min)
 """
 import hashlib
 import json
@@ -186,6 +188,56 @@ def config4_case(n_boxes=400):
             "box_seed": 0xB0C5, "boxes": boxes}
 
 
+def served_mix(dims, n, seed=0xC5C5):
+    """The served-decode request mix over the 2048^3 archive: 70% one 32^3 atom
+    at LOD0, 25% boxes with edges U[64,128] at LOD 0-1, 5% 512^3 boxes at LOD2
+    (numpy default_rng; bench.py draws the same sequence from this seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        u = rng.random()
+        if u < 0.70:
+            d = R.lod_dims(*dims, 0)
+            o = [32 * int(rng.integers(0, (d[k] + 31) // 32)) for k in range(3)]
+            e = [min(32, d[k] - o[k]) for k in range(3)]
+            lod = 0
+        elif u < 0.95:
+            lod = int(rng.integers(0, 2))
+            d = R.lod_dims(*dims, lod)
+            e = [int(min(rng.integers(64, 129), d[k])) for k in range(3)]
+            o = [int(rng.integers(0, d[k] - e[k] + 1)) for k in range(3)]
+        else:
+            lod = 2
+            d = R.lod_dims(*dims, 2)
+            e = [min(512, d[k]) for k in range(3)]
+            o = [int(rng.integers(0, d[k] - e[k] + 1)) for k in range(3)]
+        out.append((lod, (o[0], o[1], o[2], o[0] + e[0], o[1] + e[1], o[2] + e[2])))
+    return out
+
+
+def config5_case(n_reqs=200):
+    """2048^3 at target_ratio 20 (the served workload): the archive's hash and
+    the reference's decode of n_reqs requests of the served mix."""
+    dims = (2048, 2048, 2048)
+    seed = V.config_seed(5)
+    vol = V.synth(*dims, seed, threads=os.cpu_count())
+    data, q0 = R.ref_encode(vol, 20.0, threads=os.cpu_count())
+    vsha = sha(vol)
+    del vol
+    nlod = R.nlod_of(*dims)
+    a = R.RefArchive(data)
+    reqs = []
+    for lod, box in served_mix(dims, n_reqs):
+        s, out = a.decode_region(lod, box)
+        assert s == 0
+        reqs.append({"lod": lod, "box": list(box), "sha256": sha(out)})
+    a.close()
+    print(f"cfg5: q0={q0} len={len(data)}", flush=True)
+    return {"name": "cfg5_2048_t20", "kind": "synth", "dims": list(dims), "seed": seed, "target": 20.0,
+            "q0": q0, "nlod": nlod, "len": len(data), "sha256": sha(data), "volume_sha256": vsha,
+            "mix_seed": 0xC5C5, "requests": reqs}
+
+
 def main():
     big = "--big" in sys.argv
     cases = json.load(open(OUT))["cases"] if os.path.exists(OUT) and "--append" in sys.argv else []
@@ -196,6 +248,8 @@ def main():
 
     if "--cfg4" in sys.argv:
         add(config4_case())
+    elif "--cfg5" in sys.argv:
+        add(config5_case())
     elif not big or "cfg1_256_t10" not in names:
         add(synth_case("cfg1_256_t10", (256, 256, 256), V.config_seed(1), 10.0, keep=False, nboxes=10))
         add(synth_case("synth_64_t10", (64, 64, 64), 0x5EED1001, 10.0))

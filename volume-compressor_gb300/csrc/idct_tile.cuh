@@ -10,6 +10,14 @@
 
 namespace vcg {
 
+// Barrier of the NT threads that work on one tile: the whole CTA (BAR = 0), or
+// named barrier BAR when the tile's threads are only part of the CTA.
+template <int NT, int BAR>
+__device__ __forceinline__ void tile_sync() {
+    if (BAR == 0) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"r"(BAR), "r"(NT) : "memory");
+}
+
 // dequantised coefficient of raw level l at raster r (src/vc/vc.c:327-338, i32 wrap)
 __device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t *dqs, const int32_t *dqb,
                                            const uint32_t *alt) {
@@ -24,14 +32,17 @@ __device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t 
 // dequantised as they are scattered into T (32 slabs x padded 32x32, i32;
 // only the nonzero levels are touched), then one warp per slab (lane per
 // line). Ends with a barrier.
-template <int NT>
+// tid: the thread's index among the tile's NT threads. COH: the lists were
+// written during this kernel (fused decode): read them through L2.
+template <int NT, int BAR = 0, bool COH = false>
 __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, const vcd_atom &e, uint32_t c,
                                              const uint32_t *src, const uint16_t *scan, const uint32_t *band_start,
-                                             const int32_t *dqs, const int32_t *dqb, const uint32_t *alt) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+                                             const int32_t *dqs, const int32_t *dqb, const uint32_t *alt,
+                                             int tid) {
+    const int lane = tid & 31, warp = tid >> 5;
     int4 *T4 = reinterpret_cast<int4 *>(T);
     for (int i = tid; i < kTileInts / 4; i += NT) T4[i] = make_int4(0, 0, 0, 0);
-    __syncthreads();
+    tile_sync<NT, BAR>();
     if (c & kEntOverflow) {
         // slow path for streams whose list exceeded its capacity
         if (tid == 0)
@@ -50,7 +61,7 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
 #pragma unroll
             for (uint32_t j = 0; j < kB; ++j) {
                 const uint32_t i = i0 + j * NT + tid;
-                w[j] = i < n ? __ldg(src + i) : 0u;
+                w[j] = i < n ? (COH ? __ldcg(src + i) : __ldg(src + i)) : 0u;
             }
 #pragma unroll
             for (uint32_t j = 0; j < kB; ++j) r[j] = __ldg(scan + (w[j] & 0xFFFFu));
@@ -59,7 +70,7 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
                 if (i0 + j * NT + tid < n) T[tile_idx(r[j])] = dequant((int16_t)(w[j] >> 16), r[j], dqs, dqb, alt);
         }
     }
-    __syncthreads();
+    tile_sync<NT, BAR>();
     for (int kz = warp; kz < 32; kz += NT / 32) {
         int32_t *S = T + kz * kSlabPitch;
         int32_t *row = S + lane * kRowPitch, *col = S + lane;
@@ -84,7 +95,7 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
         }
         __syncwarp();
     }
-    __syncthreads();
+    tile_sync<NT, BAR>();
 }
 
 // Pass along z for column (y, x = lane): voxel values before +dc.
@@ -138,9 +149,10 @@ __device__ __forceinline__ void store_col_full(uint8_t *obase, uint64_t ox, uint
 }
 
 template <int NT>
-__device__ __forceinline__ void zero_window(uint8_t *obase, uint64_t ox, uint64_t oy, const Crop &k) {
+__device__ __forceinline__ void zero_window(uint8_t *obase, uint64_t ox, uint64_t oy, const Crop &k,
+                                            uint32_t tid) {
     const uint32_t cw = k.lx1 - k.lx0, ch = k.ly1 - k.ly0, cd = k.lz1 - k.lz0;
-    for (uint32_t i = threadIdx.x; i < cw * ch * cd; i += NT) {
+    for (uint32_t i = tid; i < cw * ch * cd; i += NT) {
         uint32_t x = i % cw, y = (i / cw) % ch, z = i / (cw * ch);
         obase[((uint64_t)z * oy + y) * ox + x] = 0;
     }

@@ -152,7 +152,7 @@ template <int NT>
 __device__ __forceinline__ void zero_all(const BatchJob &J, const UAtom &a) {
     for (uint32_t d = a.dst_begin; d < a.dst_end; ++d) {
         const BoxWin w(J.reqs[J.dst[d]], a.ax * 32, a.ay * 32, a.az * 32);
-        zero_window<NT>(w.ob, w.ox, w.oy, w.k);
+        zero_window<NT>(w.ob, w.ox, w.oy, w.k, threadIdx.x);
     }
 }
 
@@ -191,7 +191,7 @@ __device__ __forceinline__ void bf_atom_to_boxes(int32_t *T, const BatchJob &J, 
         b.pad = 0;
         bs[threadIdx.x] = b;
     }
-    idct_tile_xy<NT>(T, J.arc, e, c, J.ent + J.ent_off[u], J.scan, J.band_start, dqs, dqb, alt);
+    idct_tile_xy<NT>(T, J.arc, e, c, J.ent + J.ent_off[u], J.scan, J.band_start, dqs, dqb, alt, threadIdx.x);
     for (int y = warp; y < 32; y += NT / 32) {
         int32_t o[32];
         idct_col_z(T, y, lane, o);

@@ -33,9 +33,10 @@ __global__ void k_caps(DecodeJob J) {
     box_atom(J, t, az, ay, ax);
     vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
     uint64_t cap = 0;
-    if (e.kind == VCD_PRESENT) {
+    if (e.kind == VCD_PRESENT) {   // slots of the list, a multiple of 32 (the host's entry_cap)
         cap = 8ull * (e.len - 1) + 64ull;
         if (cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+        cap = (cap + 31) & ~31ull;
     }
     J.ent_off[t] = cap;
 }
@@ -198,6 +199,7 @@ __global__ void k_len_scatter(DecodeJob J) {
     box_atom(J, t, az, ay, ax);
     const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
     if (e.kind == VCD_PRESENT) J.order[atomicAdd(&J.sort_ctl[len_bucket(e.len)], 1u)] = (uint32_t)t;
+    else J.order[J.sort_ctl[kSortBuckets] + atomicAdd(&J.sort_ctl[kSortBuckets + 1], 1u)] = (uint32_t)t;   // after them
 }
 
 static_assert(kSortBuckets == 4 * 1024, "k_len_scan: 1024 threads x 4 counters");
@@ -272,39 +274,175 @@ static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s) {
     k_rc_decode<<<(unsigned)((J.n_atoms + G - 1) / G), 32, 0, s>>>(Jr, G, lat);
 }
 
+// Box atom t: dequantise + inverse transform + crop into the box raster, by NT
+// threads (tid = 0..NT-1) that meet at barrier BAR (tile_sync); ends with one.
+template <int NT, int BAR>
+__device__ __forceinline__ void idct_atom(const DecodeJob &J, uint64_t t, int32_t *T, const int32_t *dqs,
+                                          const int32_t *dqb, const uint32_t *alt, int tid) {
+    const int lane = tid & 31, warp = tid >> 5;
+    uint32_t az, ay, ax;
+    box_atom(J, t, az, ay, ax);
+    const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
+    Crop k;
+    const uint32_t gx = ax * 32, gy = ay * 32, gz = az * 32;
+    k.set(gx, gy, gz, J.x0, J.y0, J.z0, J.x1, J.y1, J.z1);
+    uint8_t *obase = J.out + ((uint64_t)(gz + k.lz0 - J.z0) * J.oy + (gy + k.ly0 - J.y0)) * J.ox + (gx + k.lx0 - J.x0);
+    // (BAR != 0: inside the fused decode, whose lists and counts this kernel wrote)
+    const uint32_t c = e.kind == VCD_PRESENT ? (BAR ? __ldcg(J.cnt + t) : J.cnt[t]) : kEntBad;
+    if (e.kind != VCD_PRESENT || (c & kEntBad)) {   // ABSENT / KNOWN_ZERO -> zeros
+        zero_window<NT>(obase, J.ox, J.oy, k, (uint32_t)tid);
+        return;
+    }
+    const int32_t dc = J.arc[e.off];
+    idct_tile_xy<NT, BAR, BAR != 0>(T, J.arc, e, c, J.ent + J.ent_off[t], J.scan, J.band_start, dqs, dqb, alt, tid);
+    const bool full = k.lz0 == 0 && k.lz1 == 32;
+    for (int y = warp; y < 32; y += NT / 32) {
+        int32_t o[32];
+        idct_col_z(T, y, lane, o);
+        if (full) store_col_full(obase, J.ox, J.oy, k, y, lane, o, dc);
+        else store_col(obase, J.ox, J.oy, k, y, lane, o, dc);
+    }
+    tile_sync<NT, BAR>();
+}
+
 __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
     extern __shared__ int32_t T[];   // 32 slabs x padded 32x32 (idct_tile.cuh)
     __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
     __shared__ uint32_t alt[1024];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     for (int i = tid; i < VCD_NCLASS; i += kIdctThreads) { dqs[i] = J.dq->step[i]; dqb[i] = J.dq->bias[i]; }
     for (int i = tid; i < 1024; i += kIdctThreads) alt[i] = J.alt_mask[i];
     __syncthreads();
+    for (uint64_t t = J.t_lo + blockIdx.x; t < J.t_hi; t += gridDim.x) idct_atom<kIdctThreads, 0>(J, t, T, dqs, dqb, alt, tid);
+}
 
-    for (uint64_t t = J.t_lo + blockIdx.x; t < J.t_hi; t += gridDim.x) {
-        uint32_t az, ay, ax;
-        box_atom(J, t, az, ay, ax);
-        const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
-        Crop k;
-        const uint32_t gx = ax * 32, gy = ay * 32, gz = az * 32;
-        k.set(gx, gy, gz, J.x0, J.y0, J.z0, J.x1, J.y1, J.z1);
-        uint8_t *obase = J.out + ((uint64_t)(gz + k.lz0 - J.z0) * J.oy + (gy + k.ly0 - J.y0)) * J.ox + (gx + k.lx0 - J.x0);
-        const uint32_t c = e.kind == VCD_PRESENT ? J.cnt[t] : kEntBad;
-        if (e.kind != VCD_PRESENT || (c & kEntBad)) {   // ABSENT / KNOWN_ZERO -> zeros
-            zero_window<kIdctThreads>(obase, J.ox, J.oy, k);
-            continue;
+// ---- fused decode: range decode and inverse transform in one persistent
+// kernel, one CTA per SM. Each CTA owns the entries c, c + G, c + 2G, ... of
+// the payload-length order (G CTAs), so every CTA gets the same mix of long
+// and short atoms. Its first 8 warps decode them (per-lane decoder, lane j
+// takes the CTA's entries j, j + 256, ...); whenever a lane finishes an atom
+// it publishes the atom in the CTA's queue. The other 8 warps transform the
+// queued atoms in that order (ABSENT / KNOWN_ZERO atoms are queued at the
+// start), so the transforms of finished atoms run while the coder is still busy
+// with the longer ones: the integer-multiply pipe of the transform and the ALU
+// work of the coder share the SM instead of running one after the other. Only
+// warps of the same CTA wait for one another; a wait that exceeds kFusedSpin
+// polls sets *fail and the transform warps stop.
+constexpr int kFusedRcThreads = 256;   // 8 decoding warps
+constexpr int kFusedTxThreads = 256;   // 8 transforming warps
+constexpr int kFusedThreads = kFusedRcThreads + kFusedTxThreads;
+constexpr uint32_t kQueueEmpty = 0xFFFFFFFFu;
+constexpr uint64_t kFusedSpin = 1ull << 24;   // x 256 ns sleeps: about 4 s
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// queue: G x per slots, CTA c's at [c * per, c * per + per), preset to kQueueEmpty
+__global__ void __launch_bounds__(kFusedThreads, 1) k_decode_fused(DecodeJob J, uint32_t *queue, uint32_t per,
+                                                                    uint32_t *fail) {
+    extern __shared__ int32_t T[];   // transform tile
+    __shared__ uint32_t bstart[9];
+    __shared__ uint32_t S[12 * kFusedRcThreads];
+    __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
+    __shared__ uint32_t alt[1024];
+    __shared__ uint32_t q_tail;   // slots of this CTA's queue handed out
+    __shared__ uint32_t cur[2];   // atom of the transform's current iteration (double-buffered)
+    const int tid = threadIdx.x;
+    if (tid < 9) bstart[tid] = J.band_start[tid];
+    for (int i = tid; i < VCD_NCLASS; i += kFusedThreads) { dqs[i] = J.dq->step[i]; dqb[i] = J.dq->bias[i]; }
+    for (int i = tid; i < 1024; i += kFusedThreads) alt[i] = J.alt_mask[i];
+    if (tid == 0) q_tail = 0;
+    __syncthreads();
+    const uint32_t G = gridDim.x, cta = blockIdx.x;
+    const uint32_t n = (uint32_t)J.n_atoms, n_present = J.sort_ctl[kSortBuckets];
+    const uint32_t n_cta = cta < n ? (n - 1 - cta) / G + 1 : 0;
+    const uint32_t np_cta = cta < n_present ? (n_present - 1 - cta) / G + 1 : 0;
+    uint32_t *Q = queue + (uint64_t)cta * per;
+    if (tid < kFusedRcThreads) {
+        for (uint32_t k = np_cta + tid; k < n_cta; k += kFusedRcThreads)   // nothing to decode
+            atomicExch(Q + atomicAdd(&q_tail, 1u), J.order[cta + k * G]);
+        uint32_t *Sl = S + tid;
+        uint32_t k = tid, t = 0, cap = 0;
+        bool have = false;
+        RcLane L;
+        auto start = [&]() {   // the lane's next atom, if any
+            have = k < np_cta;
+            vcd_atom e = {};
+            uint32_t *dst = J.ent;
+            if (have) {
+                t = J.order[cta + k * G];
+                uint32_t az, ay, ax;
+                box_atom(J, t, az, ay, ax);
+                e = J.atoms[job_atom(J, t, az, ay, ax)];
+                cap = 8u * (e.len - 1u) + 64u;
+                if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+                dst = J.ent + J.ent_off[t];
+            }
+            L.init(J.arc + e.off + 1, e.len - 1u, have, bstart, Sl, kFusedRcThreads, dst, cap);
+        };
+        start();
+        while (__any_sync(0xFFFFFFFFu, have)) {
+#pragma unroll
+            for (int s = 0; s < kLaneUnroll; ++s) L.step(bstart, Sl, kFusedRcThreads);
+            if (have && L.c == kLaneDone) {   // finished: counts, then publish the atom
+                const uint32_t m = L.n > cap ? cap : L.n;
+                J.cnt[t] = m | (L.n > cap ? kEntOverflow : 0u) | (L.bad ? kEntBad : 0u);
+                atomicAdd(J.nnz_total, (unsigned long long)m);
+                if (L.bad) atomicMin(J.err, t);
+                __threadfence();
+                atomicExch(Q + atomicAdd(&q_tail, 1u), t);
+                k += kFusedRcThreads;
+                start();
+            }
         }
-        const int32_t dc = J.arc[e.off];
-        idct_tile_xy<kIdctThreads>(T, J.arc, e, c, J.ent + J.ent_off[t], J.scan, J.band_start, dqs, dqb, alt);
-        const bool full = k.lz0 == 0 && k.lz1 == 32;
-        for (int y = warp; y < 32; y += kIdctThreads / 32) {
-            int32_t o[32];
-            idct_col_z(T, y, lane, o);
-            if (full) store_col_full(obase, J.ox, J.oy, k, y, lane, o, dc);
-            else store_col(obase, J.ox, J.oy, k, y, lane, o, dc);
+    } else {
+        const int tt = tid - kFusedRcThreads;
+        for (uint32_t k = 0; k < n_cta; ++k) {
+            if (tt == 0) {
+                uint32_t v = ld_acquire_u32(Q + k);
+                for (uint64_t spins = 0; v == kQueueEmpty; v = ld_acquire_u32(Q + k)) {
+                    if (++spins > kFusedSpin) {
+                        atomicExch(fail, 1u);
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+                cur[k & 1] = v;
+            }
+            tile_sync<kFusedTxThreads, 1>();
+            const uint32_t t = cur[k & 1];
+            if (t == kQueueEmpty) break;   // gave up waiting (every transform thread sees it)
+            __threadfence();
+            idct_atom<kFusedTxThreads, 1>(J, t, T, dqs, dqb, alt, tt);
         }
-        __syncthreads();
     }
+}
+
+// Fused range decode + transform of a whole box: above one atom per warp (the
+// per-lane decoder's range) with an order buffer; queue: per-CTA slots
+// (decode_fused_queue_words(n) words), fail: a zeroed word. Returns false when
+// the box takes the separate kernels instead.
+bool launch_decode_fused(const DecodeJob &J, int num_sms, cudaStream_t s, uint32_t *queue, uint32_t *fail,
+                         const StageEvents *ev) {
+    if (!J.order || !J.sort_ctl || !queue || rc_lanes_for(J.n_atoms, (uint32_t)num_sms, rc_scalar_warps()) <= 1)
+        return false;
+    const uint32_t G = (uint32_t)num_sms;
+    const uint32_t per = (uint32_t)((J.n_atoms + G - 1) / G);
+    if (ev) cudaEventRecord(ev->ev[0], s);
+    const unsigned nb = (unsigned)((J.n_atoms + 127) / 128);
+    k_caps<<<nb, 128, 0, s>>>(J);
+    launch_scan_u64(J.ent_off, J.n_atoms, 0, nullptr, s);
+    if (ev) cudaEventRecord(ev->ev[1], s);
+    launch_len_sort(J, s);
+    cudaMemsetAsync(queue, 0xFF, (size_t)G * per * 4, s);
+    if (ev) cudaEventRecord(ev->ev[2], s);
+    smem_attr((const void *)k_decode_fused, (int)kIdctSmem);
+    k_decode_fused<<<G, kFusedThreads, kIdctSmem, s>>>(J, queue, per, fail);
+    if (ev) cudaEventRecord(ev->ev[3], s);
+    return true;
 }
 
 void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cudaStream_t s) {

@@ -126,6 +126,12 @@ void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s);
 void launch_scan_u64(uint64_t *v, uint64_t n, uint64_t base, uint64_t *total, cudaStream_t s);
 // exclusive scan of the kSortBuckets length counters in place, their sum after them
 void launch_len_scan(uint32_t *sort_ctl, cudaStream_t s);
+// Range decode and inverse transform of a whole box in one kernel (k_decode_fused)
+// when the box takes the per-lane decoder and J has an order buffer: queue holds
+// n_atoms + num_sms words, fail a word that starts at zero (set if the kernel
+// gave up waiting). Records ev[0..3] like launch_decode. False: not applicable.
+bool launch_decode_fused(const DecodeJob &J, int num_sms, cudaStream_t s, uint32_t *queue, uint32_t *fail,
+                         const StageEvents *ev);
 
 // cudaFuncAttributeMaxDynamicSharedMemorySize of kernel fn, set on the calling
 // thread's current device. The attribute belongs to the device's context, not

@@ -248,6 +248,60 @@ cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out) {
 }
 
 // ---------------------------------------------------------------- archive residency
+// Device blocks of closed archives are kept for the next archive that fits
+// (at most kBlockCache blocks, each reused only for a request of at least half
+// its size), so a caller that opens and closes archives of similar size does
+// not pay cudaMalloc / cudaFree (and the synchronisation cudaFree implies) per
+// archive.
+namespace {
+constexpr int kBlockCache = 6;
+struct CachedBlock {
+    void *p;
+    size_t cap;
+};
+CachedBlock g_blocks[kBlockCache];
+pthread_mutex_t g_block_mu = PTHREAD_MUTEX_INITIALIZER;
+
+cudaError_t block_alloc(size_t bytes, void **out, size_t *cap) {
+    pthread_mutex_lock(&g_block_mu);
+    int best = -1;
+    for (int i = 0; i < kBlockCache; ++i)
+        if (g_blocks[i].p && g_blocks[i].cap >= bytes && g_blocks[i].cap / 2 <= bytes &&
+            (best < 0 || g_blocks[i].cap < g_blocks[best].cap))
+            best = i;
+    if (best >= 0) {
+        *out = g_blocks[best].p;
+        *cap = g_blocks[best].cap;
+        g_blocks[best].p = NULL;
+        pthread_mutex_unlock(&g_block_mu);
+        return cudaSuccess;
+    }
+    pthread_mutex_unlock(&g_block_mu);
+    *cap = bytes;
+    return cudaMalloc(out, bytes);
+}
+
+// p must be idle (no work of any stream still using it)
+void block_release(void *p, size_t cap) {
+    if (!p) return;
+    pthread_mutex_lock(&g_block_mu);
+    int slot = -1;
+    for (int i = 0; i < kBlockCache; ++i)
+        if (!g_blocks[i].p) { slot = i; break; }
+    if (slot < 0) {   // full: evict the smallest cached block if this one is larger
+        int small = 0;
+        for (int i = 1; i < kBlockCache; ++i)
+            if (g_blocks[i].cap < g_blocks[small].cap) small = i;
+        if (g_blocks[small].cap < cap) {
+            cudaFree(g_blocks[small].p);
+            slot = small;
+        }
+    }
+    if (slot >= 0) g_blocks[slot] = CachedBlock{p, cap};
+    else cudaFree(p);
+    pthread_mutex_unlock(&g_block_mu);
+}
+}  // namespace
 
 // Residency in two steps, so that the copy of the archive bytes runs while the
 // host resolves the atom table: begin allocates and starts the copy on the
@@ -258,8 +312,10 @@ extern "C" int vcd_upload_begin(vcd_archive **out, const uint8_t *buf, size_t le
     vcd_archive *d = (vcd_archive *)calloc(1, sizeof(vcd_archive));
     if (!d) return 3;
     cudaError_t e;
-    if ((e = cudaMalloc(&d->arc, len + 16)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(d->arc, buf, len, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+    void *blk = NULL;
+    if ((e = block_alloc(len + 16, &blk, &d->arc_cap)) != cudaSuccess ||
+        (d->arc = (uint8_t *)blk, (e = cudaMemcpyAsync(d->arc, buf, len, cudaMemcpyHostToDevice, c->stream))) !=
+            cudaSuccess ||
         (e = cudaMemsetAsync(d->arc + len, 0, 16, c->stream)) != cudaSuccess) {
         vcd_set_error("archive upload", e);
         cudaStreamSynchronize(c->stream);
@@ -275,11 +331,14 @@ extern "C" int vcd_upload_finish(vcd_archive *d, const vcd_atom *atoms, uint64_t
     vcd_ctx *c = vcd_thread_ctx();
     if (!c) return 4;
     cudaError_t e;
-    if ((e = cudaMalloc(&d->atoms, (n_atoms ? n_atoms : 1) * sizeof(vcd_atom))) != cudaSuccess ||
-        (e = cudaMemcpyAsync(d->atoms, atoms, n_atoms * sizeof(vcd_atom), cudaMemcpyHostToDevice, c->stream)) !=
+    void *blk = NULL;
+    if ((e = block_alloc((n_atoms ? n_atoms : 1) * sizeof(vcd_atom), &blk, &d->atoms_cap)) != cudaSuccess ||
+        (d->atoms = (vcd_atom *)blk,
+         (e = cudaMemcpyAsync(d->atoms, atoms, n_atoms * sizeof(vcd_atom), cudaMemcpyHostToDevice, c->stream))) !=
             cudaSuccess ||
-        (e = cudaMalloc(&d->dq, nlod * sizeof(vcd_dq))) != cudaSuccess ||
-        (e = cudaMemcpyAsync(d->dq, dq, nlod * sizeof(vcd_dq), cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+        (e = block_alloc(nlod * sizeof(vcd_dq), &blk, &d->dq_cap)) != cudaSuccess ||
+        (d->dq = (vcd_dq *)blk,
+         (e = cudaMemcpyAsync(d->dq, dq, nlod * sizeof(vcd_dq), cudaMemcpyHostToDevice, c->stream))) != cudaSuccess ||
         (e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
         vcd_set_error("archive upload", e);
         cudaStreamSynchronize(c->stream);
@@ -291,9 +350,16 @@ extern "C" int vcd_upload_finish(vcd_archive *d, const vcd_atom *atoms, uint64_t
 
 extern "C" void vcd_free_archive(vcd_archive *d) {
     if (!d) return;
-    cudaFree(d->arc);
-    cudaFree(d->atoms);
-    cudaFree(d->dq);
+    // work on this thread's stream (a failed upload's copy) ends before its
+    // blocks may serve another archive; decodes of the archive have returned
+    vcd_ctx *c = vcd_thread_ctx();
+    if (c) cudaStreamSynchronize(c->stream);
+    if (d->arc_cap) block_release(d->arc, d->arc_cap);
+    else cudaFree(d->arc);
+    if (d->atoms_cap) block_release(d->atoms, d->atoms_cap);
+    else cudaFree(d->atoms);
+    if (d->dq_cap) block_release(d->dq, d->dq_cap);
+    else cudaFree(d->dq);
     free(d);
 }
 
@@ -588,6 +654,8 @@ cudaError_t vcd_copy_from_host(vcd_ctx *c, void *dst_dev, const void *src, size_
 }
 
 // ---------------------------------------------------------------- decode
+constexpr uint64_t kFusedMaxPayload = 3072;   // mean payload bytes per PRESENT atom of a fused decode
+
 // One box decode from device bytes `arc` and atom table `atoms` (LOD raster, or
 // box order when box_table). last_ms spans from `t0` (or the first stage event).
 static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uint32_t box_table, const vcd_dq *dq,
@@ -611,8 +679,10 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     }
     p_err = p_ctl;
     void *p_ord = NULL;   // only large decodes use the per-lane range decoder (launch_rc)
+    // [sort counters][order: n][fused-decode queue: n + SMs]
     if (rc_sorts(n, (uint32_t)g_dev.num_sms) &&
-        (e = vcd_scratch(c, VCD_BUF_ORD, (n + sort_ctl_words()) * 4 + 16, &p_ord)) != cudaSuccess) {
+        (e = vcd_scratch(c, VCD_BUF_ORD, (2 * n + g_dev.num_sms + sort_ctl_words()) * 4 + 16, &p_ord)) !=
+            cudaSuccess) {
         vcd_set_error("decode scratch", e);
         return vcd_status_of(e);
     }
@@ -661,7 +731,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     // payload range keeps the exact per-atom copy below)
     // (pageable destinations take the same slabs, copied out through pinned
     // bounce chunks by host threads)
-    bool piped = false, bounce = false;
+    bool piped = false, bounce = false, fused = false;
     const uint64_t layer = (uint64_t)r->bnx * r->bny, layers = layer ? n / layer : 0;
     if (out_host && out_bytes >= (64ull << 20) && n == box_atoms && layers * layer == n && layers >= 2) {
         cudaPointerAttributes pa;
@@ -708,14 +778,23 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
             }
         }
     } else {
-        launch_decode_front(J, g_dev.num_sms, c->stream, &ev);
-        if ((e = cudaPeekAtLastError()) != cudaSuccess) {
-            vcd_set_error("decode launch (lists, range decoder)", e);
-            cudaGetLastError();
-            return vcd_status_of(e);
+        // fused only for light payloads: on GB300 a 1024^3 decode at ~4.4 KB per atom
+        // (target 10) took 12.9 ms fused against 11.6 ms for the two kernels (the
+        // transform warps take issue slots from the latency-bound coder), at ~1 KB
+        // (target 50) 5.9 against ~7 ms and at ~0.5 KB (target 100) 4.0 against 4.5
+        const bool light = r->present && r->payload_bytes <= kFusedMaxPayload * r->present;
+        fused = p_ord && light &&
+                launch_decode_fused(J, g_dev.num_sms, c->stream, J.order + n, (uint32_t *)p_ctl + 1, &ev);
+        if (!fused) {
+            launch_decode_front(J, g_dev.num_sms, c->stream, &ev);
+            if ((e = cudaPeekAtLastError()) != cudaSuccess) {
+                vcd_set_error("decode launch (lists, range decoder)", e);
+                cudaGetLastError();
+                return vcd_status_of(e);
+            }
+            launch_idct(J, g_dev.num_sms, c->stream, 0, n);
+            cudaEventRecord(ev.ev[3], c->stream);
         }
-        launch_idct(J, g_dev.num_sms, c->stream, 0, n);
-        cudaEventRecord(ev.ev[3], c->stream);
         if ((e = cudaPeekAtLastError()) != cudaSuccess) {
             vcd_set_error("decode launch (inverse transform)", e);
             cudaGetLastError();
@@ -732,13 +811,23 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
         return vcd_status_of(e);
     }
     c->last_ms = vcd_elapsed(t0 ? t0 : ev.ev[0], ev.ev[3]);
+    if (fused && (ctl_h[0] >> 32) != 0) {   // the fused kernel's transform warps gave up waiting
+        vcd_set_error("fused decode: an atom never reached the transform", cudaSuccess);
+        return 4;
+    }
     if (vcd_prof_on()) {
         const uint64_t nnz = ctl_h[1];
         vcd_prof_add("decode_place", vcd_elapsed(ev.ev[0], ev.ev[1]), n ? 2 : 0, 24 * n, 8 * n, n);
-        // (the per-lane decoder: length sort in three kernels, then the decoder)
-        vcd_prof_add("rc_decode", vcd_elapsed(ev.ev[1], ev.ev[2]), n ? (p_ord ? 4 : 1) : 0, r->payload_bytes + 16 * n, 4 * nnz,
-                     r->present);
-        vcd_prof_add("idct", vcd_elapsed(ev.ev[2], ev.ev[3]), n ? 1 : 0, 4 * nnz + 16 * n, out_bytes, n);
+        if (fused) {   // length sort (three kernels); range decode + transform in one kernel
+            vcd_prof_add("length_sort", vcd_elapsed(ev.ev[1], ev.ev[2]), 3, 16 * n, 8 * n, n);
+            vcd_prof_add("decode_fused", vcd_elapsed(ev.ev[2], ev.ev[3]), 1, r->payload_bytes + 16 * n, out_bytes,
+                         n);
+        } else {
+            // (the per-lane decoder: length sort in three kernels, then the decoder)
+            vcd_prof_add("rc_decode", vcd_elapsed(ev.ev[1], ev.ev[2]), n ? (p_ord ? 4 : 1) : 0,
+                         r->payload_bytes + 16 * n, 4 * nnz, r->present);
+            vcd_prof_add("idct", vcd_elapsed(ev.ev[2], ev.ev[3]), n ? 1 : 0, 4 * nnz + 16 * n, out_bytes, n);
+        }
     }
     const uint32_t err_h = (uint32_t)ctl_h[0];
     const uint64_t good = err_h < n ? err_h : n;   // atoms written before the first bad one

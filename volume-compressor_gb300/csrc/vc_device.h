@@ -58,6 +58,7 @@ struct vcd_archive {
     vcd_atom *atoms;    // all LODs
     vcd_dq *dq;         // per LOD
     int nlod;
+    size_t arc_cap, atoms_cap, dq_cap;   // bytes of the blocks (from the residency block cache; 0: cudaMalloc'd)
 };
 
 struct vcd_device {

@@ -429,9 +429,12 @@ done:
 // whole bypass (sign) bit, so a stream of n range-coder bytes cannot carry more
 // than 8n of them; hostile streams that would exceed it are decoded on a slow
 // path inside the kernel.
+// list slots of a PRESENT atom, a multiple of 32 (128 bytes): no two atoms'
+// lists share a cache line (k_caps places them the same way)
 static inline uint64_t entry_cap(const vcd_atom *t) {
     uint64_t c = 8ull * (t->len - 1) + 64;
-    return c > VCD_MAX_ENTRIES ? VCD_MAX_ENTRIES : c;
+    c = c > VCD_MAX_ENTRIES ? VCD_MAX_ENTRIES : c;
+    return (c + 31) & ~31ull;
 }
 
 // ---------------------------------------------------------------------------
