@@ -1232,8 +1232,10 @@ def gb300_arm(args, dist):
     peak, peak_kind = measured_peak()
     dom = max((k for k in stats if k in ("idct", "rc_decode", "decode_fused")), key=lambda k: stats[k]["ms"])
     st_ = stats[dom]
-    per_launch_bytes = (st_["bytes_read"] + st_["bytes_written"]) / max(1, st_["launches"])
-    per_launch_ms = st_["ms"] / max(1, st_["launches"])
+    # per step of the stage (one decode call): the range-decode stage is the
+    # per-lane decoder's launch after three small length-sort launches
+    per_launch_bytes = (st_["bytes_read"] + st_["bytes_written"]) / args.steps
+    per_launch_ms = st_["ms"] / args.steps
     achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
     launches = int(sum(v["launches"] for v in stats.values()))
 
@@ -1276,7 +1278,7 @@ def gb300_arm(args, dist):
     if dist.rank != 0:
         return
     roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": dram_traffic(dom, st_["units"] / max(1, st_["launches"])),
+            "frac": achieved / peak, "traffic": dram_traffic(dom, st_["units"] / args.steps),
             "peak_source": peak_kind}
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": dist.world, "steps": args.steps,

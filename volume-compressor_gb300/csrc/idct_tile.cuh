@@ -28,20 +28,38 @@ __device__ __forceinline__ int32_t dequant(int32_t l, uint32_t r, const int32_t 
     return l == 0 ? 0 : (l < 0 ? (int32_t)(0u - (uint32_t)v) : v);
 }
 
+// Scratch after the tile (kIdctTileBytes in all): the rows (kz, ky) that hold a
+// level, as one 32-bit mask per slab, the prefix of their counts over the
+// slabs, and the list of those rows.
+constexpr int kTileExtraInts = 32 + 32 + 4 + 512;
+constexpr size_t kIdctTileBytes = (size_t)(kTileInts + kTileExtraInts) * sizeof(int32_t);
+
 // Tile of one PRESENT atom after the inverse passes along x and y: levels
 // dequantised as they are scattered into T (32 slabs x padded 32x32, i32;
-// only the nonzero levels are touched), then one warp per slab (lane per
-// line). Ends with a barrier.
+// only the nonzero levels are touched). Then, by default, one warp per slab
+// (lane per row, then lane per column), all-zero slabs skipped. With COMPACT,
+// the rows that received a level are marked, the pass along x runs only on
+// those (lane per row, from a compact list: a row without a level stays zero,
+// as the reference skips zero lines, src/vc/vc.c:177) and the pass along y on
+// slabs with a marked row. COMPACT runs fewer multiplies but mixes slabs in a
+// warp (shared-memory bank conflicts) and adds barriers: measured on GB300 it
+// pays only where the transform shares the SM with the range decoder (the
+// fused decode: 1024^3 t50 5.96 -> 5.63 ms), not in the transform kernel alone
+// (t10 3.40 -> 3.50 ms). T needs kIdctTileBytes. Ends with a barrier.
 // tid: the thread's index among the tile's NT threads. COH: the lists were
 // written during this kernel (fused decode): read them through L2.
-template <int NT, int BAR = 0, bool COH = false>
+template <int NT, int BAR = 0, bool COH = false, bool COMPACT = false>
 __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, const vcd_atom &e, uint32_t c,
                                              const uint32_t *src, const uint16_t *scan, const uint32_t *band_start,
                                              const int32_t *dqs, const int32_t *dqb, const uint32_t *alt,
                                              int tid) {
     const int lane = tid & 31, warp = tid >> 5;
     int4 *T4 = reinterpret_cast<int4 *>(T);
+    uint32_t *rowmask = reinterpret_cast<uint32_t *>(T + kTileInts);
+    uint32_t *pre = rowmask + 32, *nrows = pre + 32;
+    uint16_t *rows = reinterpret_cast<uint16_t *>(nrows + 4);
     for (int i = tid; i < kTileInts / 4; i += NT) T4[i] = make_int4(0, 0, 0, 0);
+    if (tid < 32) rowmask[tid] = 0;
     tile_sync<NT, BAR>();
     if (c & kEntOverflow) {
         // slow path for streams whose list exceeded its capacity
@@ -49,6 +67,7 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
             rc_decode_levels_lane(arc + e.off + 1, e.len - 1, band_start, [&](uint32_t p, uint32_t lv) {
                 const uint32_t r = scan[p];
                 T[tile_idx(r)] = dequant((int16_t)lv, r, dqs, dqb, alt);
+                if (COMPACT) rowmask[r >> 10] |= 1u << ((r >> 5) & 31u);
             });
     } else {
         // batches of kB entries per thread: every list load of a batch is issued
@@ -67,33 +86,82 @@ __device__ __forceinline__ void idct_tile_xy(int32_t *T, const uint8_t *arc, con
             for (uint32_t j = 0; j < kB; ++j) r[j] = __ldg(scan + (w[j] & 0xFFFFu));
 #pragma unroll
             for (uint32_t j = 0; j < kB; ++j)
-                if (i0 + j * NT + tid < n) T[tile_idx(r[j])] = dequant((int16_t)(w[j] >> 16), r[j], dqs, dqb, alt);
+                if (i0 + j * NT + tid < n) {
+                    T[tile_idx(r[j])] = dequant((int16_t)(w[j] >> 16), r[j], dqs, dqb, alt);
+                    if (COMPACT) atomicOr(&rowmask[r[j] >> 10], 1u << ((r[j] >> 5) & 31u));
+                }
         }
     }
     tile_sync<NT, BAR>();
-    for (int kz = warp; kz < 32; kz += NT / 32) {
-        int32_t *S = T + kz * kSlabPitch;
-        int32_t *row = S + lane * kRowPitch, *col = S + lane;
-        int32_t v[32], o[32];
-        int any = 0;
+    if (!COMPACT) {
+        for (int kz = warp; kz < 32; kz += NT / 32) {
+            int32_t *S = T + kz * kSlabPitch;
+            int32_t *row = S + lane * kRowPitch, *col = S + lane;
+            int32_t v[32], o[32];
+            int any = 0;
 #pragma unroll
-        for (int kx = 0; kx < 32; ++kx) {
-            v[kx] = row[kx];
-            any |= v[kx];
+            for (int kx = 0; kx < 32; ++kx) {
+                v[kx] = row[kx];
+                any |= v[kx];
+            }
+            if (__any_sync(0xFFFFFFFFu, any)) {   // an all-zero slab stays zero
+                idct32_line(v, o);
+#pragma unroll
+                for (int x = 0; x < 32; ++x) row[x] = o[x];
+                __syncwarp();
+#pragma unroll
+                for (int ky = 0; ky < 32; ++ky) v[ky] = col[ky * kRowPitch];
+                idct32_line(v, o);
+                __syncwarp();
+#pragma unroll
+                for (int y = 0; y < 32; ++y) col[y * kRowPitch] = o[y];
+            }
+            __syncwarp();
         }
-        if (__any_sync(0xFFFFFFFFu, any)) {   // an all-zero slab stays zero
+        tile_sync<NT, BAR>();
+        return;
+    }
+    if (warp == 0) {   // rows before each slab's, and their total
+        const uint32_t m = __popc(rowmask[lane]);
+        uint32_t incl = m;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        pre[lane] = incl - m;
+        if (lane == 31) *nrows = incl;
+    }
+    tile_sync<NT, BAR>();
+    for (int i = tid; i < 1024; i += NT) {
+        const uint32_t m = rowmask[i >> 5], bit = (uint32_t)i & 31u;
+        if ((m >> bit) & 1u) rows[pre[i >> 5] + __popc(m & ((1u << bit) - 1u))] = (uint16_t)i;
+    }
+    tile_sync<NT, BAR>();
+    const uint32_t nr = *nrows;
+    for (uint32_t b = (uint32_t)warp * 32u; b < nr; b += NT) {   // along x, listed rows only
+        const uint32_t idx = b + (uint32_t)lane;
+        if (idx < nr) {
+            const uint32_t ri = rows[idx];
+            int32_t *row = T + (ri >> 5) * kSlabPitch + (ri & 31u) * kRowPitch;
+            int32_t v[32], o[32];
+#pragma unroll
+            for (int kx = 0; kx < 32; ++kx) v[kx] = row[kx];
             idct32_line(v, o);
 #pragma unroll
             for (int x = 0; x < 32; ++x) row[x] = o[x];
-            __syncwarp();
-#pragma unroll
-            for (int ky = 0; ky < 32; ++ky) v[ky] = col[ky * kRowPitch];
-            idct32_line(v, o);
-            __syncwarp();
-#pragma unroll
-            for (int y = 0; y < 32; ++y) col[y * kRowPitch] = o[y];
         }
-        __syncwarp();
+    }
+    tile_sync<NT, BAR>();
+    for (int kz = warp; kz < 32; kz += NT / 32) {   // along y, slabs with a row
+        if (!rowmask[kz]) continue;   // an all-zero slab stays zero
+        int32_t *col = T + kz * kSlabPitch + lane;
+        int32_t v[32], o[32];
+#pragma unroll
+        for (int ky = 0; ky < 32; ++ky) v[ky] = col[ky * kRowPitch];
+        idct32_line(v, o);
+#pragma unroll
+        for (int y = 0; y < 32; ++y) col[y * kRowPitch] = o[y];
     }
     tile_sync<NT, BAR>();
 }

@@ -14,7 +14,7 @@
 
 namespace vcg {
 
-constexpr size_t kTileSmem = kTileBytes;   // the butterfly's padded tile (idct_tile.cuh)
+constexpr size_t kTileSmem = kIdctTileBytes;   // the butterfly's padded tile + its row lists (idct_tile.cuh)
 
 // Persistent over the batch's distinct atoms (their number is read from device
 // memory) while the policy keeps one atom per warp (rc_lanes_for gives 1):
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(NT, 1) k_idct_batch(BatchJob J) {
 // values leave the three-piece range take the butterfly, so every result is
 // the reference's.
 constexpr size_t kImmaSmem = 2 * 3 * 32768;   // two buffers of three piece planes
-static_assert(kImmaSmem >= kTileBytes, "an atom redone with the butterfly reuses the planes as its tile");
+static_assert(kImmaSmem >= kIdctTileBytes, "an atom redone with the butterfly reuses the planes as its tile");
 
 template <int NT>
 __global__ void __launch_bounds__(NT, 1) k_idct_batch_imma(BatchJob J) {

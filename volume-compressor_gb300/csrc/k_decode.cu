@@ -24,7 +24,7 @@
 namespace vcg {
 
 constexpr int kIdctThreads = 512;   // 16 warps per atom (measured faster than 8 on GB300)
-constexpr size_t kIdctSmem = kTileBytes;
+constexpr size_t kIdctSmem = kIdctTileBytes;
 
 __global__ void k_caps(DecodeJob J) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -294,7 +294,8 @@ __device__ __forceinline__ void idct_atom(const DecodeJob &J, uint64_t t, int32_
         return;
     }
     const int32_t dc = J.arc[e.off];
-    idct_tile_xy<NT, BAR, BAR != 0>(T, J.arc, e, c, J.ent + J.ent_off[t], J.scan, J.band_start, dqs, dqb, alt, tid);
+    idct_tile_xy<NT, BAR, BAR != 0, BAR != 0>(T, J.arc, e, c, J.ent + J.ent_off[t], J.scan, J.band_start, dqs, dqb,
+                                               alt, tid);
     const bool full = k.lz0 == 0 && k.lz1 == 32;
     for (int y = warp; y < 32; y += NT / 32) {
         int32_t o[32];
