@@ -196,8 +196,10 @@ class Clocks:
 LIMITER = {
     "decode_fused": "the range decoders' dependency chains (8 warps per SM) beside the transform's integer multiplies "
                     "(8 warps per SM) in one kernel",
-    "rc_decode": "dependency chain of each serial range decoder: 44 % issue active, DRAM under 1 % busy (ncu)",
-    "idct": "integer pipes of the inverse passes: 52 % issue active, DRAM 6 % busy (ncu)",
+    "rc_decode": "instructions and dependency chain of the per-lane range decoder (one decision per step): "
+                 "ALU pipe 55 %, DRAM about 1 % busy (ncu)",
+    "idct": "integer multiply-adds of the inverse passes: FMA-heavy pipe 62 % busy, 53 % of its measured IMAD "
+            "rate over the transform's 1.06 M IMAD per atom; DRAM 6 % busy (ncu)",
 }
 
 
@@ -1030,7 +1032,7 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
     dv.free()
     a = vc.Archive(data)
     assert a.make_resident() == 0
-    cfg = {"device_budget": 2 << 30, "max_batch": 1024, "workers": 3}
+    cfg = {"device_budget": 2 << 30, "max_batch": 1024, "workers": int(os.environ.get("VC_BENCH_SERVER_WORKERS", "3"))}
     rng = np.random.default_rng(0x5E5E)
     warm = served_mix(a, rng, 64)   # first batches tune the launch shape and build graphs
     wo = [np.empty(_box_bytes(b), np.uint8) for _, b in warm]

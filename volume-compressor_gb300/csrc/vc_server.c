@@ -8,13 +8,14 @@
 // decodes them in one batched pass (each distinct atom once, cropped into
 // every box; vcg_decode_regions) and releases their budget; a batch of one
 // request takes the plain decode path (vc_decode_region), which has the lower
-// latency. A large request (kBigVoxels or more) runs alone through the plain
-// path when it is the oldest request waiting, on at most workers - 1 workers at
-// a time, so that one worker always serves the small requests and a small
-// request never waits behind a large one's decode. Requests that arrive while
-// batches are on the GPU join the next batch of whichever worker frees up
-// first, so batches from different workers overlap on the device. Each result
-// is exactly what vc_decode_region returns for that request alone.
+// latency. Large requests (kBigVoxels or more) are batched only with each
+// other, when the oldest waiting request is a large one, on at most
+// workers - 1 workers at a time, so that one worker always serves the small
+// requests and a small request never waits behind a large one's decode.
+// Requests that arrive while batches are on the GPU join the next batch of
+// whichever worker frees up first, so batches from different workers overlap
+// on the device. Each result is exactly what vc_decode_region returns for that
+// request alone.
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -102,20 +103,23 @@ static void *worker(void *arg) {
             }
             s->q_small -= k;
         } else if (s->q_big && s->big_running < big_slots) {
-            for (uint64_t t = s->head; t < s->n; ++t) {
+            // the oldest large request, with the other large ones waiting while
+            // memory and the batch limit allow (large boxes of one LOD often
+            // share atoms, which the batch decodes once)
+            for (uint64_t t = s->head; t < s->n && k < s->max_batch; ++t) {
                 srv_req *r = slot(s, t);
-                if (r->state != 0) continue;
-                if (s->in_use + r->cost <= s->budget || s->in_use == 0) {
-                    r->state = 1;
-                    batch[0] = r->req;
-                    tix[0] = t;
-                    take = r->cost;
-                    k = 1;
-                    big = 1;
-                    s->q_big -= 1;
-                    s->big_running += 1;
-                }
-                break;
+                if (r->state != 0 || !r->big) continue;
+                if (s->in_use + take + r->cost > s->budget && (k > 0 || s->in_use > 0)) break;
+                r->state = 1;
+                batch[k] = r->req;
+                tix[k] = t;
+                take += r->cost;
+                ++k;
+            }
+            if (k) {
+                big = 1;
+                s->q_big -= k;
+                s->big_running += 1;
             }
         }
         while (s->head < s->n && slot(s, s->head)->state != 0) ++s->head;
