@@ -236,6 +236,16 @@ int   vcg_memset(void *dst, int v, size_t bytes);
 int   vcg_sync(void);
 int   vcg_device_info(int *num_sms, int *cc_major, int *cc_minor);
 int   vcg_device_memory(size_t *free_bytes, size_t *total_bytes);   // cudaMemGetInfo of the library's device
+
+// Allocation-failure injection, for tests: with n > 0, the n-th device or
+// pinned-host allocation the library makes from now on fails as if the device
+// were out of memory (once); n <= 0 turns it off. Returns the previous state:
+// allocations still to go before the failure, -1 if the failure happened, 0
+// if off. Arming (n > 0) also frees the device blocks kept from closed
+// archives. A call that meets the failure returns VC_ERR_OOM (or NULL / -1 where
+// it returns a handle or ticket), or succeeds where it has a path that needs no
+// new allocation, and leaves the library usable.
+int64_t vcg_debug_fail_alloc(int64_t n);
 const char *vcg_last_error(void);
 
 #ifdef __cplusplus

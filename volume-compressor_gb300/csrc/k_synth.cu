@@ -113,11 +113,11 @@ VC_API int vcg_synth_device(const syn_cfg *cfg_host, uint8_t *out_dev) {
     syn_cfg *c = NULL;
     float *a = NULL, *b = NULL;
     uint8_t *mask = NULL;
-    cudaError_t e = cudaMalloc(&c, sizeof(syn_cfg));
+    cudaError_t e = vcd_malloc((void **)&c, sizeof(syn_cfg));
     if (e == cudaSuccess) e = cudaMemcpyAsync(c, cfg_host, sizeof(syn_cfg), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMalloc(&a, plane * (slab + 6) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&b, plane * (slab + 6) * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&mask, plane * slab + 16);
+    if (e == cudaSuccess) e = vcd_malloc((void **)&a, plane * (slab + 6) * sizeof(float));
+    if (e == cudaSuccess) e = vcd_malloc((void **)&b, plane * (slab + 6) * sizeof(float));
+    if (e == cudaSuccess) e = vcd_malloc((void **)&mask, plane * slab + 16);
     const int grid = g_dev.num_sms * 8;
     for (uint32_t z0 = 0; e == cudaSuccess && z0 < cfg_host->nz; z0 += slab) {
         uint32_t z1 = z0 + slab < cfg_host->nz ? z0 + slab : cfg_host->nz;
@@ -147,7 +147,7 @@ VC_API void *vcg_alloc(size_t bytes) {
     VCD_SCOPE();
     if (vcd_init() != 0) return NULL;
     void *p = NULL;
-    return cudaMalloc(&p, bytes ? bytes : 1) == cudaSuccess ? p : NULL;
+    return vcd_malloc((void **)&p, bytes ? bytes : 1) == cudaSuccess ? p : NULL;
 }
 VC_API void vcg_free(void *p) {
     VCD_SCOPE();
@@ -157,7 +157,7 @@ VC_API void *vcg_alloc_host(size_t bytes) {
     VCD_SCOPE();
     if (vcd_init() != 0) return NULL;
     void *p = NULL;
-    return cudaMallocHost(&p, bytes ? bytes : 1) == cudaSuccess ? p : NULL;
+    return vcd_malloc_host((void **)&p, bytes ? bytes : 1) == cudaSuccess ? p : NULL;
 }
 VC_API void vcg_free_host(void *p) {
     VCD_SCOPE();

@@ -43,7 +43,7 @@ static void init_once(void) {
     vcd_tables *t = (vcd_tables *)malloc(sizeof(vcd_tables));
     vch_tables(t);
     memcpy(g_dev.band_start, t->band_start, sizeof g_dev.band_start);
-    if ((e = cudaMalloc(&g_dev.tables, sizeof(vcd_tables))) != cudaSuccess ||
+    if ((e = cudaMalloc(&g_dev.tables, sizeof(vcd_tables))) != cudaSuccess ||   // process set-up: not injected
         (e = cudaMemcpy(g_dev.tables, t, sizeof(vcd_tables), cudaMemcpyHostToDevice)) != cudaSuccess) {
         vcd_set_error("table upload", e);
         free(t);
@@ -215,6 +215,53 @@ extern "C" __attribute__((visibility("default"))) void vcg_set_rc_scalar_warps(i
     __atomic_store_n(&g_rc_scalar_warps, v, __ATOMIC_RELAXED);
 }
 
+// ---------------------------------------------------------------- allocation-failure injection
+// g_fail_alloc > 0: allocations left before one fails; -1: that failure
+// happened; 0: off. Tests use it to show that every allocation failure comes
+// back as a status and leaves the library usable.
+static int64_t g_fail_alloc;
+
+static bool injected_failure(void) {
+    int64_t v = __atomic_load_n(&g_fail_alloc, __ATOMIC_ACQUIRE);
+    while (v > 0) {
+        const int64_t nv = v == 1 ? -1 : v - 1;
+        if (__atomic_compare_exchange_n(&g_fail_alloc, &v, nv, false, __ATOMIC_ACQ_REL, __ATOMIC_ACQUIRE))
+            return nv == -1;
+    }
+    return false;
+}
+
+namespace {
+bool block_trim(void);
+}
+
+// cudaMalloc that, when the device is out of memory, first gives back the
+// cached blocks of closed archives and tries once more
+cudaError_t vcd_malloc(void **p, size_t bytes) {
+    if (injected_failure()) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation && block_trim()) {
+        cudaGetLastError();
+        e = cudaMalloc(p, bytes);
+    }
+    if (e != cudaSuccess) cudaGetLastError();   // not sticky: clear it for the next call
+    return e;
+}
+
+cudaError_t vcd_malloc_host(void **p, size_t bytes) {
+    if (injected_failure()) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMallocHost(p, bytes);
+    if (e != cudaSuccess) cudaGetLastError();
+    return e;
+}
+
+// Arming also empties the cache of archive blocks, so that the allocations a
+// call makes do not depend on the archives closed before it.
+extern "C" __attribute__((visibility("default"))) int64_t vcg_debug_fail_alloc(int64_t n) {
+    if (n > 0) block_trim();
+    return __atomic_exchange_n(&g_fail_alloc, n > 0 ? n : 0, __ATOMIC_ACQ_REL);
+}
+
 // grow-only scratch buffer `slot` of the calling thread
 cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out) {
     if (bytes == 0) bytes = 16;
@@ -226,7 +273,7 @@ cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out) {
             c->cap[slot] = 0;
         }
         size_t want = bytes + bytes / 8;
-        cudaError_t e = cudaMalloc(&c->buf[slot], want);
+        cudaError_t e = vcd_malloc((void **)&c->buf[slot], want);
         if (e != cudaSuccess) return e;
         c->cap[slot] = want;
     }
@@ -239,7 +286,7 @@ cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out) {
         if (c->pinned) cudaFreeHost(c->pinned);
         c->pinned = NULL;
         c->pinned_cap = 0;
-        cudaError_t e = cudaMallocHost(&c->pinned, bytes);
+        cudaError_t e = vcd_malloc_host((void **)&c->pinned, bytes);
         if (e != cudaSuccess) return e;
         c->pinned_cap = bytes;
     }
@@ -278,7 +325,7 @@ cudaError_t block_alloc(size_t bytes, void **out, size_t *cap) {
     }
     pthread_mutex_unlock(&g_block_mu);
     *cap = bytes;
-    return cudaMalloc(out, bytes);
+    return vcd_malloc((void **)out, bytes);
 }
 
 // p must be idle (no work of any stream still using it)
@@ -300,6 +347,20 @@ void block_release(void *p, size_t cap) {
     if (slot >= 0) g_blocks[slot] = CachedBlock{p, cap};
     else cudaFree(p);
     pthread_mutex_unlock(&g_block_mu);
+}
+
+// frees every cached block; true if there was one
+bool block_trim(void) {
+    bool any = false;
+    pthread_mutex_lock(&g_block_mu);
+    for (int i = 0; i < kBlockCache; ++i)
+        if (g_blocks[i].p) {
+            cudaFree(g_blocks[i].p);
+            g_blocks[i] = CachedBlock{NULL, 0};
+            any = true;
+        }
+    pthread_mutex_unlock(&g_block_mu);
+    return any;
 }
 }  // namespace
 
@@ -886,7 +947,7 @@ extern "C" int vcd_upload_dq(vcd_archive **out, const vcd_dq *dq, int nlod) {
     vcd_archive *d = (vcd_archive *)calloc(1, sizeof(vcd_archive));
     if (!d) return 3;
     cudaError_t e;
-    if ((e = cudaMalloc(&d->dq, nlod * sizeof(vcd_dq))) != cudaSuccess ||
+    if ((e = vcd_malloc((void **)&d->dq, nlod * sizeof(vcd_dq))) != cudaSuccess ||
         (e = cudaMemcpy(d->dq, dq, nlod * sizeof(vcd_dq), cudaMemcpyHostToDevice)) != cudaSuccess) {
         vcd_set_error("dequantisation tables", e);
         vcd_free_archive(d);
@@ -912,7 +973,7 @@ extern "C" int vcd_stage_reserve(size_t bytes, uint8_t **host) {
         c->stage_host = NULL;
         c->stage_cap = 0;
         const size_t want = bytes + bytes / 4;
-        if ((e = cudaMallocHost(&c->stage_host, want)) != cudaSuccess) {
+        if ((e = vcd_malloc_host((void **)&c->stage_host, want)) != cudaSuccess) {
             c->stage_host = NULL;
             vcd_set_error("staging", e);
             return vcd_status_of(e);

@@ -70,6 +70,10 @@ struct vcd_device {
 extern vcd_device g_dev;
 vcd_ctx *vcd_thread_ctx(void);
 cudaError_t vcd_scratch(vcd_ctx *c, int slot, size_t bytes, void **out);
+// cudaMalloc / cudaMallocHost of the library, through the allocation-failure
+// injector (vcg_debug_fail_alloc)
+cudaError_t vcd_malloc(void **p, size_t bytes);
+cudaError_t vcd_malloc_host(void **p, size_t bytes);
 cudaError_t vcd_pinned(vcd_ctx *c, size_t bytes, void **out);
 // the context's second stream with its slab and bounce-slot events, created on first use; NULL if that fails
 cudaStream_t vcd_side_stream(vcd_ctx *c);

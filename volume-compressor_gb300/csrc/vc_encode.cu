@@ -468,7 +468,7 @@ extern "C" int vcd_encode_segments(const vcd_seg *segs, int nseg, const float *q
                 if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
                 size_t want = (total + bytes) + (total + bytes) / 2 + (1 << 20);
                 uint8_t *np_ = NULL;
-                if ((e = cudaMallocHost(&np_, want)) != cudaSuccess) break;
+                if ((e = vcd_malloc_host((void **)&np_, want)) != cudaSuccess) break;
                 if (c->wpin) {
                     memcpy(np_, c->wpin, total);
                     cudaFreeHost(c->wpin);

@@ -155,7 +155,7 @@ struct vc_archive {
     float base_q[VC_NLOD];
     // device residency, built on first decode
     pthread_mutex_t mu;
-    int resident;           // 0 not yet, 1 ok, -1 failed
+    int resident;           // 0 not (yet), 1 ok
     vcd_atom *atoms;        // all LODs, LOD-major, raster (az, ay, ax) within a LOD
     uint64_t lod_base[VC_NLOD + 1];
     vcd_archive *dev;
@@ -366,14 +366,18 @@ static int pull_whole(vc_archive *a) {
 
 // Resolve every atom of every LOD once, validate payload ranges, and move the
 // archive bytes plus the table into device memory.
-static int make_resident(vc_archive *a) {
+// A failed attempt (no device memory, a read that failed) leaves the archive
+// not resident, so a later call tries again; the status says why it failed.
+static vc_status make_resident(vc_archive *a) {
     pthread_mutex_lock(&a->mu);
-    if (a->resident) { int r = a->resident; pthread_mutex_unlock(&a->mu); return r > 0 ? 0 : -1; }
-    int rc = -1;
+    if (a->resident) { pthread_mutex_unlock(&a->mu); return VC_OK; }
+    vc_status rc = VC_ERR_IO;
+    int e;
     if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); goto done; }
-    if (!a->buf && pull_whole(a) != 0) { pthread_mutex_unlock(&a->mu); return -1; }
-    if (vcd_upload_begin(&a->dev, a->buf, a->len) != 0) {   // the copy runs during the walk below
+    if (!a->buf && pull_whole(a) != 0) goto done;
+    if ((e = vcd_upload_begin(&a->dev, a->buf, a->len)) != 0) {   // the copy runs during the walk below
         report("archive upload failed: %s", vcd_last_error());
+        rc = (vc_status)e;
         goto done;
     }
     uint64_t total = 0;
@@ -384,7 +388,7 @@ static int make_resident(vc_archive *a) {
     }
     a->lod_base[a->nlod] = total;
     a->atoms = (vcd_atom *)calloc(total ? total : 1, sizeof(vcd_atom));
-    if (!a->atoms) goto done;
+    if (!a->atoms) { rc = VC_ERR_OOM; goto done; }
     vcd_dq dq[VC_NLOD];
     for (int l = 0; l < a->nlod; ++l) {
         vc_dims d = lod_dims_of(a->d0, l);
@@ -410,17 +414,20 @@ static int make_resident(vc_archive *a) {
                             }
                 }
     }
-    if (vcd_upload_finish(a->dev, a->atoms, total, dq, a->nlod) != 0) {
+    if ((e = vcd_upload_finish(a->dev, a->atoms, total, dq, a->nlod)) != 0) {
         report("archive upload failed: %s", vcd_last_error());
+        rc = (vc_status)e;
         goto done;
     }
-    rc = 0;
+    rc = VC_OK;
 done:
-    if (rc != 0 && a->dev) {
-        vcd_free_archive(a->dev);   // also waits for a copy still in flight
+    if (rc != VC_OK) {
+        if (a->dev) vcd_free_archive(a->dev);   // also waits for a copy still in flight
         a->dev = NULL;
+        free(a->atoms);
+        a->atoms = NULL;
     }
-    a->resident = rc == 0 ? 1 : -1;
+    __atomic_store_n(&a->resident, rc == VC_OK ? 1 : 0, __ATOMIC_RELEASE);
     pthread_mutex_unlock(&a->mu);
     return rc;
 }
@@ -505,14 +512,15 @@ static void *fetch_worker(void *p) {
     }
 }
 
-static int stream_device(vc_archive *a) {   // dequantisation tables on the device, once
+static vc_status stream_device(vc_archive *a) {   // dequantisation tables on the device, once
     pthread_mutex_lock(&a->mu);
-    int rc = 0;
+    vc_status rc = VC_OK;
+    int e;
     if (!a->sdev) {
         vcd_dq dq[VC_NLOD];
         for (int l = 0; l < a->nlod; ++l) vch_dq_consts(a->base_q[l], &dq[l]);
-        if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); rc = -1; }
-        else if (vcd_upload_dq(&a->sdev, dq, a->nlod) != 0) { report("%s", vcd_last_error()); rc = -1; }
+        if (vcd_init() != 0) { report("no usable CUDA device: %s", vcd_last_error()); rc = VC_ERR_IO; }
+        else if ((e = vcd_upload_dq(&a->sdev, dq, a->nlod)) != 0) { report("%s", vcd_last_error()); rc = (vc_status)e; }
     }
     pthread_mutex_unlock(&a->mu);
     return rc;
@@ -520,7 +528,8 @@ static int stream_device(vc_archive *a) {   // dequantisation tables on the devi
 
 static vc_status decode_box_streamed(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev,
                                      int bad_as_empty, uint64_t *n_present) {
-    if (stream_device(a) != 0) return VC_ERR_IO;
+    vc_status sd = stream_device(a);
+    if (sd != VC_OK) return sd;
     const vc_dims d = lod_dims_of(a->d0, lod);
     vcd_region r;
     memset(&r, 0, sizeof r);
@@ -674,7 +683,8 @@ out:
 static vc_status decode_box(vc_archive *a, int lod, vc_box b, uint8_t *out, uint8_t *out_dev) {
     if (a->read && __atomic_load_n(&a->resident, __ATOMIC_ACQUIRE) != 1)
         return decode_box_streamed(a, lod, b, out, out_dev, 0, NULL);
-    if (make_resident(a) != 0) return VC_ERR_IO;
+    vc_status rs = make_resident(a);
+    if (rs != VC_OK) return rs;
     vc_dims d = lod_dims_of(a->d0, lod);
     vcd_region r;
     memset(&r, 0, sizeof r);
@@ -769,7 +779,8 @@ VC_API vc_status vcg_decode_regions(vc_archive *a, uint32_t n, const vcg_region_
     VCD_SCOPE();
     if (!a || (n && (!reqs || !status))) return VC_ERR_RANGE;
     if (n == 0) return VC_OK;
-    if (make_resident(a) != 0) return VC_ERR_IO;
+    vc_status rs = make_resident(a);
+    if (rs != VC_OK) return rs;
     const uint64_t total_atoms = a->lod_base[a->nlod];
     int32_t *uid = (int32_t *)malloc((total_atoms ? total_atoms : 1) * sizeof(int32_t));
     vcd_boxreq *br = (vcd_boxreq *)calloc(n, sizeof(vcd_boxreq));
@@ -895,7 +906,7 @@ done:
 VC_API vc_status vcg_make_resident(vc_archive *a) {
     VCD_SCOPE();
     if (!a) return VC_ERR_RANGE;
-    return make_resident(a) == 0 ? VC_OK : VC_ERR_IO;
+    return make_resident(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -1079,7 +1090,8 @@ VC_API vc_status vcg_repack_v2(vc_archive *a, uint8_t **out_archive, size_t *out
     if (!a || !out_archive || !out_len) return VC_ERR_RANGE;
     *out_archive = NULL;
     *out_len = 0;
-    if (make_resident(a) != 0) return VC_ERR_IO;
+    vc_status rs = make_resident(a);
+    if (rs != VC_OK) return rs;
     uint64_t prefix[VC_NLOD + 1], total_regions = 0;
     for (int l = 0; l < a->nlod; ++l) {
         uint32_t z, y, x;

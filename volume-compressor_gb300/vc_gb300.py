@@ -32,7 +32,7 @@ VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_re
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
-               "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_device_memory", "vcg_last_error", "vcg_profile_enable",
+               "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_device_memory", "vcg_debug_fail_alloc", "vcg_last_error", "vcg_profile_enable",
                "vcg_profile_read", "vcg_last_call_ms"]
 
 
@@ -191,6 +191,8 @@ def lib():
         L.vcg_memset.argtypes = [P, ctypes.c_int, ctypes.c_size_t]
         L.vcg_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
         L.vcg_device_memory.argtypes = [ctypes.POINTER(ctypes.c_size_t)] * 2
+        L.vcg_debug_fail_alloc.argtypes = [ctypes.c_int64]
+        L.vcg_debug_fail_alloc.restype = ctypes.c_int64
         L.vcg_last_error.restype = ctypes.c_char_p
         L.vcg_decode_atoms_noalloc.argtypes = [P, ctypes.c_size_t, P, P, ctypes.c_uint32, ctypes.c_float, P]
         L.vcg_decode_regions.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int, P]
