@@ -21,8 +21,19 @@ constexpr size_t kTileSmem = kIdctTileBytes;   // the butterfly's padded tile + 
 // scalar decoder. With more atoms, k_rc_batch_lanes takes them instead (or,
 // without its order buffer, the lockstep decoder here).
 constexpr int kRcBatchThreads = 128;
+// Stream bytes a warp stages in shared memory for the latency decoder, when the
+// batch's capacity keeps it on that decoder (launched with these slices).
+constexpr uint32_t kBatchStage = 40u * 1024u;
+constexpr uint32_t kBatchStageSmem = (kRcBatchThreads / 32) * kBatchStage;
+
+__device__ __forceinline__ uint32_t dynamic_smem_bytes() {
+    uint32_t v;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(v));
+    return v;
+}
 
 __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
+    extern __shared__ uint8_t bstage[];
     __shared__ uint32_t bstart[9];
     if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
     __syncthreads();
@@ -30,16 +41,45 @@ __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
     const uint32_t G = rc_lanes_for(n, J.sms, J.rc_scalar_warps);
     if (G > 1 && J.order) return;   // k_rc_batch_lanes decodes this batch
     const uint32_t lane = threadIdx.x & 31u;
-    if (G == 1 && lane != 0) return;
+    // latency decoder with the stream staged by the whole warp
+    const bool staged = G == 1 && n <= 4u * J.sms && dynamic_smem_bytes() >= kBatchStageSmem;
+    if (G == 1 && !staged && lane != 0) return;
+    uint8_t *stage = bstage + (threadIdx.x >> 5) * kBatchStage;
+    const uint32_t slot = G == 1 ? 0u : lane;
     const uint64_t nwarps = (uint64_t)gridDim.x * (kRcBatchThreads / 32);
     for (uint64_t w = ((uint64_t)blockIdx.x * kRcBatchThreads + threadIdx.x) >> 5; w * G < n; w += nwarps) {
-        const uint64_t u = w * G + lane;
+        const uint64_t u = w * G + slot;
         bool active = false;
         vcd_atom e = {};
-        if (lane < G && u < n) {
+        if (slot < G && u < n) {
             e = J.atoms[J.ua[u].idx];
             active = e.kind == VCD_PRESENT;
-            if (!active) J.cnt[u] = 0;
+            if (!active && lane == 0) J.cnt[u] = 0;
+        }
+        bool in_smem = false;
+        if (staged) {
+            __syncwarp();   // lane 0 is done with the slice (its previous atom)
+            const uint32_t len = active ? e.len - 1u : 0u;
+            in_smem = active && len < kBatchStage;
+            if (in_smem) {   // 8 independent byte loads per lane in flight, then their stores
+                const uint8_t *src = J.arc + e.off + 1;
+                for (uint32_t i0 = 0; i0 < len; i0 += 8u * 32u) {
+                    uint32_t b[8];
+#pragma unroll
+                    for (uint32_t k = 0; k < 8; ++k) {
+                        const uint32_t i = i0 + k * 32u + lane;
+                        b[k] = i < len ? (uint32_t)__ldg(src + i) : 0u;
+                    }
+#pragma unroll
+                    for (uint32_t k = 0; k < 8; ++k) {
+                        const uint32_t i = i0 + k * 32u + lane;
+                        if (i < len) stage[i] = (uint8_t)b[k];
+                    }
+                }
+                if (lane == 0) stage[len] = 0;
+            }
+            __syncwarp();
+            if (lane != 0) continue;
         }
         uint32_t cap = 0, cnt = 0;
         uint32_t *dst = J.ent;
@@ -55,7 +95,8 @@ __global__ void __launch_bounds__(kRcBatchThreads) k_rc_batch(BatchJob J) {
         int bad = 0;
         if (G == 1) {
             // up to one atom per SM sub-partition the latency decoder, else the compact scalar one
-            if (active && n <= 4u * J.sms) bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1, bstart, sink);
+            if (in_smem) bad = rc_decode_levels_sm(stage, e.len - 1, bstart, sink);
+            else if (active && n <= 4u * J.sms) bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1, bstart, sink);
             else if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
         } else {
             bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart, sink);
@@ -381,7 +422,11 @@ static void launch_rc(const BatchJob &J, int num_sms, uint32_t max_ua, cudaStrea
         const uint64_t lg = ((uint64_t)max_ua + kBatchLaneThreads - 1) / kBatchLaneThreads;
         k_rc_batch_lanes<<<(unsigned)(lg < 1 ? 1 : lg), kBatchLaneThreads, 0, s>>>(J);
     }
-    k_rc_batch<<<grid, kRcBatchThreads, 0, s>>>(J);
+    // capacity within the latency decoder's range: stage the streams (one CTA
+    // per SM at most, with a warp per atom)
+    const bool stage = J.rc_scalar_warps && max_ua <= slots;
+    if (stage) smem_attr((const void *)k_rc_batch, (int)kBatchStageSmem);
+    k_rc_batch<<<grid, kRcBatchThreads, stage ? kBatchStageSmem : 0, s>>>(J);
 }
 
 template <int NT>

@@ -89,29 +89,64 @@ __global__ void __launch_bounds__(1024) k_scan_u64(uint64_t *v, uint64_t n, uint
     if (tid == 0 && total) *total = carry_s;
 }
 
+// Stream bytes the latency path stages in shared memory (with the zero byte
+// after them, within the 48 KiB a launch may take without opting in; four
+// such CTAs per SM at most).
+constexpr uint32_t kLatStage = 40u * 1024u;
+
 // One warp per CTA, G atoms per warp (rc_lanes_for): G = 1 runs a scalar
 // decoder on lane 0 (the latency decoder when `lat`), G > 1 the lockstep
 // decoder on lanes 0..G-1. With J.order (G = 1 only), CTA i decodes the i-th
-// atom of the payload-length order.
+// atom of the payload-length order. With `lat` the whole warp first copies the
+// atom's stream into shared memory (kLatStage bytes of dynamic shared memory:
+// streams that do not fit are read from global memory by
+// rc_decode_levels_lat).
 __global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G, uint32_t lat) {
+    extern __shared__ uint8_t stage[];
     __shared__ uint32_t bstart[9];
     if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
     __syncthreads();
     const uint32_t lane = threadIdx.x;
-    if (G == 1 && lane != 0) return;
-    uint64_t t = (uint64_t)blockIdx.x * G + lane;
+    const bool staged = G == 1 && lat;
+    if (G == 1 && !staged && lane != 0) return;
+    const uint32_t slot = G == 1 ? 0u : lane;   // (G = 1: every lane of a staging warp takes lane 0's atom)
+    uint64_t t = (uint64_t)blockIdx.x * G + slot;
     if (J.order) {
         if (t >= J.sort_ctl[kSortBuckets]) return;
         t = J.order[t];
     }
     bool active = false;
     vcd_atom e = {};
-    if (lane < G && t < J.n_atoms) {
+    if (slot < G && t < J.n_atoms) {
         uint32_t az, ay, ax;
         box_atom(J, t, az, ay, ax);
         e = J.atoms[job_atom(J, t, az, ay, ax)];
         active = e.kind == VCD_PRESENT;
-        if (!active) J.cnt[t] = 0;
+        if (!active && lane == 0) J.cnt[t] = 0;
+    }
+    bool in_smem = false;
+    if (staged) {
+        const uint32_t len = active ? e.len - 1u : 0u;
+        in_smem = active && len < kLatStage;
+        if (in_smem) {   // 8 independent byte loads per lane in flight, then their stores
+            const uint8_t *src = J.arc + e.off + 1;
+            for (uint32_t i0 = 0; i0 < len; i0 += 8u * 32u) {
+                uint32_t b[8];
+#pragma unroll
+                for (uint32_t k = 0; k < 8; ++k) {
+                    const uint32_t i = i0 + k * 32u + lane;
+                    b[k] = i < len ? (uint32_t)__ldg(src + i) : 0u;
+                }
+#pragma unroll
+                for (uint32_t k = 0; k < 8; ++k) {
+                    const uint32_t i = i0 + k * 32u + lane;
+                    if (i < len) stage[i] = (uint8_t)b[k];
+                }
+            }
+            if (lane == 0) stage[len] = 0;
+            __syncwarp();
+        }
+        if (lane != 0) return;
     }
     uint32_t cap = 0, n = 0;
     uint32_t *dst = J.ent;
@@ -127,7 +162,8 @@ __global__ void __launch_bounds__(32) k_rc_decode(DecodeJob J, uint32_t G, uint3
     };
     int bad = 0;
     if (G == 1) {
-        if (active && lat) bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1, bstart, sink);
+        if (in_smem) bad = rc_decode_levels_sm(stage, e.len - 1, bstart, sink);
+        else if (active && lat) bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1, bstart, sink);
         else if (active) bad = rc_decode_levels_lane(J.arc + e.off + 1, e.len - 1, bstart, sink);
     } else {
         bad = rc_decode_levels_warp(J.arc + e.off + 1, active ? e.len - 1 : 0u, active, bstart, sink);
@@ -270,8 +306,8 @@ static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s) {
         Jr.order = nullptr;
         Jr.sort_ctl = nullptr;
     }
-    const uint32_t lat = J.n_atoms <= 4ull * (uint64_t)num_sms ? 1u : 0u;
-    k_rc_decode<<<(unsigned)((J.n_atoms + G - 1) / G), 32, 0, s>>>(Jr, G, lat);
+    const uint32_t lat = G == 1 && J.n_atoms <= 4ull * (uint64_t)num_sms ? 1u : 0u;
+    k_rc_decode<<<(unsigned)((J.n_atoms + G - 1) / G), 32, lat ? kLatStage + 16 : 0, s>>>(Jr, G, lat);
 }
 
 // Box atom t: dequantise + inverse transform + crop into the box raster, by NT
