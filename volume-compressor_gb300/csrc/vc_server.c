@@ -8,10 +8,12 @@
 // decodes them in one batched pass (each distinct atom once, cropped into
 // every box; vcg_decode_regions) and releases their budget; a batch of one
 // request takes the plain decode path (vc_decode_region), which has the lower
-// latency. Large requests (kBigVoxels or more) are batched only with each
-// other, when the oldest waiting request is a large one, on at most
-// workers - 1 workers at a time, so that one worker always serves the small
-// requests and a small request never waits behind a large one's decode.
+// latency. Large requests (kBigVoxels or more) run, when the oldest waiting
+// request is a large one, on at most workers - 1 workers at a time, so that one
+// worker always serves the small requests and a small request never waits
+// behind a large one's decode; the waiting large requests are shared out over
+// the free large-request workers, each batch taking its share (one each while
+// there are as many workers as requests).
 // Requests that arrive while batches are on the GPU join the next batch of
 // whichever worker frees up first, so batches from different workers overlap
 // on the device. Each result is exactly what vc_decode_region returns for that
@@ -103,10 +105,15 @@ static void *worker(void *arg) {
             }
             s->q_small -= k;
         } else if (s->q_big && s->big_running < big_slots) {
-            // the oldest large request, with the other large ones waiting while
-            // memory and the batch limit allow (large boxes of one LOD often
-            // share atoms, which the batch decodes once)
-            for (uint64_t t = s->head; t < s->n && k < s->max_batch; ++t) {
+            // the waiting large requests are shared out over the free
+            // large-request slots: this worker takes the oldest and, while
+            // memory and the batch limit allow, its share of the others (large
+            // boxes of one LOD often share atoms, which a batch decodes once;
+            // one large request per worker while there are as many workers)
+            const uint64_t free_slots = (uint64_t)(big_slots - s->big_running);
+            const uint64_t share = (s->q_big + free_slots - 1) / free_slots;
+            const uint32_t kmax = share < s->max_batch ? (uint32_t)share : s->max_batch;
+            for (uint64_t t = s->head; t < s->n && k < kmax; ++t) {
                 srv_req *r = slot(s, t);
                 if (r->state != 0 || !r->big) continue;
                 if (s->in_use + take + r->cost > s->budget && (k > 0 || s->in_use > 0)) break;
