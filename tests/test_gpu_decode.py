@@ -249,3 +249,29 @@ def test_large_decode_into_pageable_memory(vc, gpu):
         assert a.decode_region_device(0, box, dbuf) == vc.VC_OK
         assert np.array_equal(host, dbuf.download(nb)), box
         dbuf.free()
+
+
+@pytest.mark.gpu
+def test_latency_decoder_streams_staged_and_not(vc, oracle, gpu):
+    """Boxes of a few atoms take the latency decoder, which stages an atom's
+    stream in 40 KiB of shared memory and reads longer streams from global
+    memory: a noise volume coded at the smallest q has streams on both sides of
+    that limit; every atom, and a box of them, must equal the oracle."""
+    vol = np.random.default_rng(0x1A7).integers(0, 256, (64, 64, 96)).astype(np.uint8)
+    vol[:, :, 64:] //= 16   # a quieter third: shorter streams
+    s, data = vc.encode_q(vol, 1.0, [0.05] * 8)
+    assert s == 0
+    a, o = vc.Archive(data), oracle.Archive(data)
+    lens = []
+    for az in range(2):
+        for ay in range(2):
+            for ax in range(3):
+                lens.append(a.payload_range(0, az, ay, ax)[2])
+                s1, g = a.decode_atom(0, ax, ay, az)
+                s2, r = o.decode_atom(0, ax, ay, az)
+                assert s1 == s2 == 0 and np.array_equal(g, r), (az, ay, ax)
+    assert min(lens) < 40 * 1024 <= max(lens), lens
+    box = (0, 0, 0, 96, 64, 64)
+    s1, g = a.decode_region(0, box)
+    s2, r = o.decode_region(0, box)
+    assert s1 == s2 == 0 and np.array_equal(g, r)

@@ -356,9 +356,13 @@ __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
 // ---- fused decode: range decode and inverse transform in one persistent
 // kernel, one CTA per SM. Each CTA owns the entries c, c + G, c + 2G, ... of
 // the payload-length order (G CTAs), so every CTA gets the same mix of long
-// and short atoms. Its first 8 warps decode them (per-lane decoder, lane j
-// takes the CTA's entries j, j + 256, ...); whenever a lane finishes an atom
-// it publishes the atom in the CTA's queue. The other 8 warps transform the
+// and short atoms. Its first 8 warps decode them: the CTA's head (entry c, its
+// longest atom) on one lane of the 8th warp with the latency decoder (a
+// decision in about 50 ns against about 110 ns for a step of the per-lane
+// decoder in a full warp, so the longest atoms no longer set the coder's end),
+// the others with the per-lane decoder on 7 warps (lane j takes the CTA's
+// entries 1 + j, 1 + j + 224, ...); whenever an atom is decoded it is published
+// in the CTA's queue. The other 8 warps transform the
 // queued atoms in that order (ABSENT / KNOWN_ZERO atoms are queued at the
 // start), so the transforms of finished atoms run while the coder is still busy
 // with the longer ones: the integer-multiply pipe of the transform and the ALU
@@ -366,6 +370,7 @@ __global__ void __launch_bounds__(kIdctThreads, 1) k_idct(DecodeJob J) {
 // warps of the same CTA wait for one another; a wait that exceeds kFusedSpin
 // polls sets *fail and the transform warps stop.
 constexpr int kFusedRcThreads = 256;   // 8 decoding warps
+constexpr int kFusedLaneThreads = kFusedRcThreads - 32;   // 7 of them per-lane; the 8th: the CTA's head atom
 constexpr int kFusedTxThreads = 256;   // 8 transforming warps
 constexpr int kFusedThreads = kFusedRcThreads + kFusedTxThreads;
 constexpr uint32_t kQueueEmpty = 0xFFFFFFFFu;
@@ -401,8 +406,32 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_decode_fused(DecodeJob J, 
     if (tid < kFusedRcThreads) {
         for (uint32_t k = np_cta + tid; k < n_cta; k += kFusedRcThreads)   // nothing to decode
             atomicExch(Q + atomicAdd(&q_tail, 1u), J.order[cta + k * G]);
+        if (tid >= kFusedLaneThreads) {   // the head: the CTA's longest atom, alone on one lane
+            if (tid == kFusedLaneThreads && np_cta) {
+                const uint32_t t = J.order[cta];
+                uint32_t az, ay, ax;
+                box_atom(J, t, az, ay, ax);
+                const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];
+                uint32_t cap = 8u * (e.len - 1u) + 64u;
+                if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+                uint32_t *dst = J.ent + J.ent_off[t];
+                uint32_t cnt = 0;
+                auto sink = [&](uint32_t p, uint32_t lv) {
+                    if (cnt < cap) dst[cnt] = p | (lv << 16);
+                    ++cnt;
+                };
+                const int bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1u, bstart, sink);
+                const uint32_t m = cnt > cap ? cap : cnt;
+                J.cnt[t] = m | (cnt > cap ? kEntOverflow : 0u) | (bad ? kEntBad : 0u);
+                atomicAdd(J.nnz_total, (unsigned long long)m);
+                if (bad) atomicMin(J.err, t);
+                __threadfence();
+                atomicExch(Q + atomicAdd(&q_tail, 1u), t);
+            }
+            return;
+        }
         uint32_t *Sl = S + tid;
-        uint32_t k = tid, t = 0, cap = 0;
+        uint32_t k = 1u + (uint32_t)tid, t = 0, cap = 0;   // the CTA's entries after its head
         bool have = false;
         RcLane L;
         auto start = [&]() {   // the lane's next atom, if any
@@ -431,7 +460,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_decode_fused(DecodeJob J, 
                 if (L.bad) atomicMin(J.err, t);
                 __threadfence();
                 atomicExch(Q + atomicAdd(&q_tail, 1u), t);
-                k += kFusedRcThreads;
+                k += kFusedLaneThreads;
                 start();
             }
         }
