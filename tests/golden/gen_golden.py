@@ -215,13 +215,48 @@ def served_mix(dims, n, seed=0xC5C5):
     return out
 
 
+def present_atoms(vol):
+    """The atoms of a volume whose dims are multiples of 32 that hold a nonzero
+    voxel, (N, 32, 32, 32) in raster order, gathered one atom layer at a time
+    (memory: the volume plus the present atoms)."""
+    nz, ny, nx = vol.shape
+    acy, acx = ny // 32, nx // 32
+
+    def layer(az):
+        return np.ascontiguousarray(
+            vol[az * 32:az * 32 + 32].reshape(32, acy, 32, acx, 32).transpose(1, 3, 0, 2, 4)).reshape(-1, 32, 32, 32)
+
+    counts = [int(layer(az).reshape(acy * acx, -1).any(axis=1).sum()) for az in range(nz // 32)]
+    pa = np.empty((sum(counts), 32, 32, 32), np.uint8)
+    k = 0
+    for az in range(nz // 32):
+        a = layer(az)
+        a = a[a.reshape(a.shape[0], -1).any(axis=1)]
+        pa[k:k + a.shape[0]] = a
+        k += a.shape[0]
+    return pa
+
+
 def config5_case(n_reqs=200):
     """2048^3 at target_ratio 20 (the served workload): the archive's hash and
-    the reference's decode of n_reqs requests of the served mix."""
+    the reference's decode of n_reqs requests of the served mix. The volume is
+    generated in slabs and the rate control gathers the present atoms once
+    (refcodec.rate_control's rule, rate_control_atoms), so that the host needs
+    about twice the volume in memory, not four times."""
     dims = (2048, 2048, 2048)
+    nx, ny, nz = dims
     seed = V.config_seed(5)
-    vol = V.synth(*dims, seed, threads=os.cpu_count())
-    data, q0 = R.ref_encode(vol, 20.0, threads=os.cpu_count())
+    vol = np.empty((nz, ny, nx), np.uint8)
+    for z0 in range(0, nz, 128):
+        vol[z0:z0 + 128] = V.synth(nx, ny, nz, seed, threads=os.cpu_count(), z0=z0, z1=min(nz, z0 + 128))
+    print("cfg5: volume", flush=True)
+    lods = R.pyramid(vol)
+    pa = present_atoms(vol)
+    q0, _, _ = R.rate_control_atoms(pa, 20.0, threads=os.cpu_count())
+    del pa
+    print(f"cfg5: q0={q0}", flush=True)
+    data = R.write_archive(lods, dims, 20.0, R.lod_qs(q0, len(lods)))
+    del lods
     vsha = sha(vol)
     del vol
     nlod = R.nlod_of(*dims)

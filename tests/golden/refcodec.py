@@ -136,8 +136,12 @@ def rate_control(vol, target, threads=8):
     """Present-atom bisection over float bit patterns in [0.05, 4096] (24 steps)."""
     atoms = atoms_of(vol).reshape(-1, 32, 32, 32)
     present = atoms.reshape(atoms.shape[0], -1).any(axis=1)
-    pa = atoms[present]
-    npres = int(present.sum())
+    return rate_control_atoms(atoms[present], target, threads)
+
+
+def rate_control_atoms(pa, target, threads=8):
+    """rate_control on the present atoms already gathered, (N, 32, 32, 32) u8."""
+    npres = int(pa.shape[0])
     if npres == 0:
         return 1.0, 0, 0
     target = float(np.float32(target))
