@@ -1073,6 +1073,18 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
     arrivals = np.cumsum(rng.exponential(1.0 / rates[-1], verify_n))
     outs = [np.empty(_box_bytes(b), np.uint8) for _, b in reqs]
     _serve_stream(a, reqs, arrivals, outs, cfg)
+    # the reference's decode of the same archive: the golden requests served
+    import hashlib
+    g = golden_named("cfg5_2048_t20")
+    arc_ok = None if g is None else g["sha256"] == hashlib.sha256(data).hexdigest()
+    ref_ok, ref_n = (None if g is None else False), 0
+    if arc_ok:
+        greqs = [(r["lod"], tuple(r["box"])) for r in g["requests"]]
+        gouts = [np.empty(_box_bytes(b), np.uint8) for _, b in greqs]
+        _serve_stream(a, greqs, np.zeros(len(greqs)), gouts, cfg)
+        ref_ok = all(hashlib.sha256(o.tobytes()).hexdigest() == r["sha256"] for o, r in zip(gouts, g["requests"]))
+        ref_n = len(greqs)
+        del gouts
     a.close()
     # every served output against the CPU's decode of the same request (the
     # CPU baseline's all-threads pass); one thread on the first requests
@@ -1087,7 +1099,9 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
     return {"workload": "2048^3 at target_ratio 20 resident in HBM; Poisson arrivals; 70% 32^3 atoms LOD0, "
                         "25% boxes U[64,128]^3 LOD0-1, 5% 512^3 LOD2; host outputs",
             "q0": q0, "archive_bytes": len(data), "server": cfg, "plain_threads": cfg["workers"],
-            "sweep": sweep, "bit_exact_all_outputs_vs_cpu": ok, "verified_requests": verify_n, "cpu_baseline": cpu}
+            "sweep": sweep, "bit_exact_all_outputs_vs_cpu": ok, "verified_requests": verify_n,
+            "bit_exact_vs_reference": {"archive": arc_ok, "requests": ref_ok, "requests_checked": ref_n},
+            "cpu_baseline": cpu}
 
 
 # ---------------------------------------------------------------- arms
