@@ -1040,7 +1040,7 @@ def config5_served(rates=(100, 300, 1000, 3000), seconds=1.5, max_requests=3000,
     big_pool = [np.empty(512 ** 3, np.uint8) for _ in range(8)]
     sweep = []
     for rate in rates:
-        m = int(min(max_requests, max(600, rate * seconds)))   # at least ~30 large requests per rate
+        m = int(min(max_requests, max(1500, rate * seconds)))   # at least ~75 large requests per rate
         reqs = served_mix(a, rng, m)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, m))
         outs, k = [], 0

@@ -9,11 +9,11 @@
 // every box; vcg_decode_regions) and releases their budget; a batch of one
 // request takes the plain decode path (vc_decode_region), which has the lower
 // latency. Large requests (kBigVoxels or more) run, when the oldest waiting
-// request is a large one, on at most workers - 1 workers at a time, so that one
-// worker always serves the small requests and a small request never waits
-// behind a large one's decode; the waiting large requests are shared out over
-// the free large-request workers, each batch taking its share (one each while
-// there are as many workers as requests).
+// request is a large one, on at most workers - 1 workers at a time while small
+// requests wait, so that one worker is left for them (on every worker while
+// none waits); the waiting large requests are shared out over the free
+// large-request workers, each batch taking its share (one each while there are
+// as many workers as requests).
 // Requests that arrive while batches are on the GPU join the next batch of
 // whichever worker frees up first, so batches from different workers overlap
 // on the device. Each result is exactly what vc_decode_region returns for that
@@ -92,7 +92,9 @@ static void *worker(void *arg) {
         int big = 0;
         while (s->head < s->n && slot(s, s->head)->state != 0) ++s->head;
         const int oldest_big = s->head < s->n && slot(s, s->head)->big;
-        if (s->q_small && !(oldest_big && s->big_running < big_slots)) {
+        // (every worker may take a large request while no small one waits)
+        const int slots_now = s->q_small ? big_slots : s->nworkers;
+        if (s->q_small && !(oldest_big && s->big_running < slots_now)) {
             for (uint64_t t = s->head; t < s->n && k < s->max_batch; ++t) {
                 srv_req *r = slot(s, t);
                 if (r->state != 0 || r->big) continue;
@@ -104,13 +106,13 @@ static void *worker(void *arg) {
                 ++k;
             }
             s->q_small -= k;
-        } else if (s->q_big && s->big_running < big_slots) {
+        } else if (s->q_big && s->big_running < slots_now) {
             // the waiting large requests are shared out over the free
             // large-request slots: this worker takes the oldest and, while
             // memory and the batch limit allow, its share of the others (large
             // boxes of one LOD often share atoms, which a batch decodes once;
             // one large request per worker while there are as many workers)
-            const uint64_t free_slots = (uint64_t)(big_slots - s->big_running);
+            const uint64_t free_slots = (uint64_t)(slots_now - s->big_running);
             const uint64_t share = (s->q_big + free_slots - 1) / free_slots;
             const uint32_t kmax = share < s->max_batch ? (uint32_t)share : s->max_batch;
             for (uint64_t t = s->head; t < s->n && k < kmax; ++t) {
