@@ -49,6 +49,7 @@ def args_parse():
     p.add_argument("--no-ds", action="store_true", help="skip the exporter-downscale measurement")
     p.add_argument("--no-writer", action="store_true", help="skip the writer-append measurement")
     p.add_argument("--no-sweep", action="store_true", help="skip the config-2 target / LOD sweep")
+    p.add_argument("--no-atom", action="store_true", help="skip the single-atom random-access measurement")
     p.add_argument("--dct-size", type=int, default=1024, help="edge of the DCT-forms volume")
     p.add_argument("--dct-reps", type=int, default=3, help="timed calls per DCT form and direction (0: one call)")
     p.add_argument("--detail", default=os.path.join(ROOT, "gpurun_out", "bench_detail.json"),
@@ -634,6 +635,63 @@ def config2_sweep(dvol, dims, peak, targets=(10.0, 50.0, 100.0)):
         row["decode_lods"] = lods
         row["lods_match_reference"] = all(lod_ok) if g else None
         res[f"t{int(t)}"] = row
+    return res
+
+
+def atom_latency(dvol, dims, target=20.0, n=50, warm=10):
+    """Random access to one 32^3 atom: the volume encoded at `target`, the
+    archive resident in device memory, and n random LOD0 atoms (after `warm`
+    untimed ones) decoded one call at a time through vc_decode_atom into host
+    memory: wall time per call, the call's device time and its stages. Beside
+    it (unless VC_BENCH_NO_CPU=1), the same atoms decoded by one host thread
+    with the oracle's vc_decode_atom (a scalar C restatement of the
+    reference's), whose bytes every GPU atom must equal."""
+    import numpy as np
+    import vc_gb300 as vc
+    s, data, q0 = vc.encode_device(dvol, dims, target)
+    assert s == 0, vc.last_error()
+    a = vc.Archive(data)
+    assert a.make_resident() == 0
+    _, (lx, ly, lz) = a.lod_dims(0)
+    rng = np.random.default_rng(7)
+    atoms = [(int(rng.integers(0, (lx + 31) // 32)), int(rng.integers(0, (ly + 31) // 32)),
+              int(rng.integers(0, (lz + 31) // 32))) for _ in range(warm + n)]
+    out = np.zeros(32768, np.uint8)
+    for ax, ay, az in atoms[:warm]:
+        assert a.decode_atom(0, ax, ay, az, out)[0] == 0
+    wall, dev, got = [], [], []
+    vc.profile_enable(True)
+    vc.profile_read(reset=True)
+    for ax, ay, az in atoms[warm:]:
+        t0 = time.perf_counter()
+        s, _ = a.decode_atom(0, ax, ay, az, out)
+        wall.append((time.perf_counter() - t0) * 1e3)
+        assert s == 0
+        dev.append(vc.last_call_ms())
+        got.append(out.copy())
+    st = vc.profile_read(reset=True)
+    vc.profile_enable(False)
+    lens = [a.payload_range(0, az, ay, ax)[2] for ax, ay, az in atoms[warm:]]
+    a.close()
+    res = {"target_ratio": target, "q0": q0, "atoms": n, "mean_payload_bytes": float(np.mean(lens)),
+           "wall_ms_p50": _pct(wall, 0.5), "wall_ms_p99": _pct(wall, 0.99),
+           "device_ms_p50": _pct(dev, 0.5),
+           "stages_ms_per_call": {k: v["ms"] / n for k, v in st.items()},
+           "launches_per_call": sum(v["launches"] for v in st.values()) / n}
+    if os.environ.get("VC_BENCH_NO_CPU") != "1":
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oraclelib
+        o = oraclelib.Archive(data)
+        cpu, same = [], True
+        for (ax, ay, az), g in zip(atoms[warm:], got):
+            t0 = time.perf_counter()
+            s, ref = o.decode_atom(0, ax, ay, az)
+            cpu.append((time.perf_counter() - t0) * 1e3)
+            same = same and s == 0 and np.array_equal(ref, g)
+        o.close()
+        res["cpu_one_thread"] = {"kind": "port", "cores": 1, "ms_p50": _pct(cpu, 0.5), "ms_p99": _pct(cpu, 0.99),
+                                 "sample": "the same atoms, oracle vc_decode_atom, one host thread"}
+        res["bit_exact_vs_oracle"] = bool(same)
     return res
 
 
@@ -1270,9 +1328,11 @@ def gb300_arm(args, dist):
         if lod0_ok is None:
             lod0_ok = bool(np.array_equal(out.download(nbytes), ref_out.ravel()))
 
-    sweep = ds = None
+    sweep = ds = atom = None
     if dist.rank == 0 and not args.no_sweep:
         sweep = config2_sweep(dvol, dims, peak)
+    if dist.rank == 0 and not args.no_atom:
+        atom = atom_latency(dvol, dims)
     if dist.rank == 0 and not args.no_ds:
         ds = downscale_bench(dvol, dims, peak)
     writer = None
@@ -1333,7 +1393,8 @@ def gb300_arm(args, dist):
     if cpu:
         detail["cpu_baseline"] = cpu
     for key, val in (("batched_regions", batched), ("served_regions", served), ("dct_forms", dct),
-                     ("config2_sweep", sweep), ("exporter_downscale", ds), ("writer_append", writer)):
+                     ("config2_sweep", sweep), ("atom_latency", atom), ("exporter_downscale", ds),
+                     ("writer_append", writer)):
         if val:
             detail[key] = val
     emit(line, detail, args.detail)
