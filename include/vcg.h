@@ -57,6 +57,14 @@ vc_status vcg_set_batch_shape(int rc_scalar_warps, int transform_threads, int tr
 // default (8: measured on GB300, the per-lane decoder wins from 3,000-5,000
 // atoms on, depending on the atoms' sizes).
 void vcg_set_rc_scalar_warps(int w);
+// The per-lane decoder's n longest atoms (by payload length) each get a warp of
+// their own running the latency-tuned decoder, on a second stream beside it
+// (process-wide; results do not depend on it). The longest atoms set the
+// per-lane decoder's time, and the latency decoder takes about half the time
+// per decision; whether that shortens the decode depends on which SM
+// sub-partitions the solo warps land on, which the launch does not control.
+// n = 0 (the default): none; n < 0 restores the default.
+void vcg_set_rc_solo(int n);
 
 // Decode server: continuous batching against one resident archive. Requests
 // queue with vcg_server_submit; `workers` threads (each with its own stream)

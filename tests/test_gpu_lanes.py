@@ -3,7 +3,9 @@ ordered by payload length) takes every decode of more than a few thousand
 atoms. Here it is forced on for every decode (range-decoder policy 0) and must
 give the reference's bits on the stored golden archives, and the oracle's
 statuses and bytes on corrupt and truncated ones, including a stream with an
-over-long escape prefix (malformed: VC_ERR_FORMAT)."""
+over-long escape prefix (malformed: VC_ERR_FORMAT). Every case runs with no
+solo atoms, with the 3 longest atoms on latency-decoder warps of their own,
+and with every atom on one."""
 import hashlib
 import struct
 
@@ -21,11 +23,13 @@ def sha(b):
     return hashlib.sha256(bytes(b)).hexdigest()
 
 
-@pytest.fixture
-def lanes(vc, gpu):
+@pytest.fixture(params=[0, 3, 1 << 30], ids=["solo0", "solo3", "solo_all"])
+def lanes(vc, gpu, request):
     vc.lib().vcg_set_rc_scalar_warps(0)
+    vc.lib().vcg_set_rc_solo(request.param)
     yield
     vc.lib().vcg_set_rc_scalar_warps(-1)
+    vc.lib().vcg_set_rc_solo(-1)
 
 
 @pytest.mark.parametrize("name", STORED)

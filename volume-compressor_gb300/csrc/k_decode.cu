@@ -277,6 +277,48 @@ __global__ void __launch_bounds__(kLaneThreads) k_rc_lanes(DecodeJob J) {
     if (L.bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
 }
 
+// Solo atoms: the first n atoms of the length order (the longest payloads)
+// each get a warp of their own whose lane 0 runs the latency decoder, on a
+// second stream beside k_rc_lanes, which takes the atoms after them. The
+// longest atoms set the per-lane decoder's time (every lane steps at about the
+// same pace, whatever its atom, bound by its own dependency chain), and the
+// latency decoder's chain is about twice as fast per decision while its one
+// lane takes about a third of a sub-partition's issue slots. Off by default
+// (vcg_set_rc_solo): measured on GB300 (1024^3 at target 10, range decode
+// 8.26 ms without) it gave 7.88 ms with 76 solo atoms in one process and
+// 8.41 ms in another, 8.0-8.3 ms with 152-608, and once 15.4 ms when the two
+// kernels ran one after the other: the gain depends on where the solo warps
+// land.
+__global__ void __launch_bounds__(32) k_rc_solo(DecodeJob J, uint32_t n) {
+    __shared__ uint32_t bstart[9];
+    if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
+    __syncthreads();
+    const uint32_t k = blockIdx.x;
+    if (threadIdx.x != 0 || k >= n || k >= J.sort_ctl[kSortBuckets]) return;
+    const uint64_t t = J.order[k];
+    uint32_t az, ay, ax;
+    box_atom(J, t, az, ay, ax);
+    const vcd_atom e = J.atoms[job_atom(J, t, az, ay, ax)];   // PRESENT: the order puts those first
+    uint32_t cap = 8u * (e.len - 1u) + 64u;
+    if (e.len - 1u > VCD_MAX_ENTRIES / 8u || cap > VCD_MAX_ENTRIES) cap = VCD_MAX_ENTRIES;
+    uint32_t *dst = J.ent + J.ent_off[t];
+    uint32_t m = 0;
+    auto sink = [&](uint32_t p, uint32_t lv) {
+        if (m < cap) dst[m] = p | (lv << 16);
+        ++m;
+    };
+    const int bad = rc_decode_levels_lat(J.arc + e.off + 1, e.len - 1u, bstart, sink);
+    J.cnt[t] = (m > cap ? cap : m) | (m > cap ? kEntOverflow : 0u) | (bad ? kEntBad : 0u);
+    atomicAdd(J.nnz_total, (unsigned long long)(m > cap ? cap : m));
+    if (bad) atomicMin(J.err, (uint32_t)(t < 0xFFFFFFFFull ? t : 0xFFFFFFFEull));
+}
+
+// ctl[kSortBuckets + 2] = the PRESENT atoms left to the per-lane warps after n solo atoms
+__global__ void k_solo_split(uint32_t *ctl, uint32_t n) {
+    const uint32_t np = ctl[kSortBuckets];
+    ctl[kSortBuckets + 2] = np - (n < np ? n : np);
+}
+
 void launch_len_scan(uint32_t *sort_ctl, cudaStream_t s) { k_len_scan<<<1, 1024, 0, s>>>(sort_ctl); }
 
 static void launch_len_sort(const DecodeJob &J, cudaStream_t s) {
@@ -291,14 +333,30 @@ static void launch_len_sort(const DecodeJob &J, cudaStream_t s) {
 //   up to one atom per SM sub-partition: latency decoder, one atom per warp;
 //   up to rc_scalar_warps() per sub-partition: scalar decoder, one atom per
 //     warp, longest payload first (the tail is the shortest atoms);
-//   above: the per-lane decoder over atoms sorted by payload length.
+//   above: the per-lane decoder over atoms sorted by payload length, the
+//     rc_solo_for() longest on the latency decoder (k_rc_solo, a warp each,
+//     on the second stream of ev, between its fork and join events).
 // Without an order buffer (no-alloc path) the unsorted forms are used.
-static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s) {
+static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s, const StageEvents *ev) {
     const uint32_t G = rc_lanes_for(J.n_atoms, (uint32_t)num_sms, rc_scalar_warps());
     const bool sorted = J.order && J.sort_ctl && rc_sorts(J.n_atoms, (uint32_t)num_sms);
     if (sorted) launch_len_sort(J, s);
     if (G > 1 && sorted) {
-        k_rc_lanes<<<(unsigned)((J.n_atoms + kLaneThreads - 1) / kLaneThreads), kLaneThreads, 0, s>>>(J);
+        const uint32_t ns = ev && ev->side && ev->fork && ev->join ? rc_solo_for(J.n_atoms, (uint32_t)num_sms) : 0u;
+        DecodeJob Jl = J;
+        if (ns) {
+            // (fewer PRESENT atoms than ns: k_solo_split's count is 0 and the
+            // shifted order is not read)
+            k_solo_split<<<1, 1, 0, s>>>(J.sort_ctl, ns);
+            cudaEventRecord(ev->fork, s);
+            cudaStreamWaitEvent(ev->side, ev->fork, 0);
+            k_rc_solo<<<ns, 32, 0, ev->side>>>(J, ns);
+            cudaEventRecord(ev->join, ev->side);
+            Jl.order = J.order + ns;
+            Jl.sort_ctl = J.sort_ctl + 2;   // Jl.sort_ctl[kSortBuckets]: the per-lane count
+        }
+        k_rc_lanes<<<(unsigned)((J.n_atoms - ns + kLaneThreads - 1) / kLaneThreads), kLaneThreads, 0, s>>>(Jl);
+        if (ns) cudaStreamWaitEvent(s, ev->join, 0);
         return;
     }
     DecodeJob Jr = J;
@@ -528,7 +586,7 @@ void launch_idct(const DecodeJob &J, int num_sms, cudaStream_t s, uint64_t t_lo,
 
 void launch_decode_lists(const DecodeJob &J, int num_sms, cudaStream_t s) {
     if (!J.n_atoms) return;
-    launch_rc(J, num_sms, s);
+    launch_rc(J, num_sms, s, nullptr);
     launch_idct(J, num_sms, s, 0, J.n_atoms);
 }
 
@@ -540,7 +598,7 @@ void launch_decode_front(const DecodeJob &J, int num_sms, cudaStream_t s, const 
         launch_scan_u64(J.ent_off, J.n_atoms, 0, nullptr, s);
     }
     if (ev) cudaEventRecord(ev->ev[1], s);
-    if (J.n_atoms) launch_rc(J, num_sms, s);
+    if (J.n_atoms) launch_rc(J, num_sms, s, ev);
     if (ev) cudaEventRecord(ev->ev[2], s);
 }
 

@@ -48,6 +48,10 @@ __host__ __device__ inline uint64_t job_atom(const DecodeJob &J, uint64_t t, uin
 // range decoder, ev[2] before the inverse transform, ev[3] after it.
 struct StageEvents {
     cudaEvent_t ev[4];
+    // optional: a second stream with two events for work beside the range
+    // decode (the solo atoms of rc_solo_for); null: none
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 __host__ __device__ inline void box_atom(const DecodeJob &J, uint64_t t, uint32_t &az, uint32_t &ay,
@@ -111,6 +115,16 @@ __host__ __device__ inline bool rc_sorts(uint64_t n_atoms, uint32_t sms) { retur
 
 // policy of the plain decode path (vcg_set_rc_scalar_warps)
 uint32_t rc_scalar_warps();
+// longest atoms of a per-lane decode that get a latency-decoder warp each
+// (vcg_set_rc_solo); rc_solo_for: how many a decode of n box atoms gets (0 when
+// it does not run the per-lane decoder)
+constexpr uint32_t kRcSoloDefault = 0;
+uint32_t rc_solo_atoms();
+inline uint32_t rc_solo_for(uint64_t n_atoms, uint32_t sms) {
+    if (rc_lanes_for(n_atoms, sms, rc_scalar_warps()) <= 1 || !rc_sorts(n_atoms, sms)) return 0;
+    const uint32_t k = rc_solo_atoms();
+    return (uint64_t)k < n_atoms ? k : (uint32_t)n_atoms;
+}
 // mid (optional): recorded between the range decode and the transform
 void launch_batch(const BatchJob &J, const BatchShape &shape, int num_sms, uint32_t max_ua, cudaStream_t s,
                   cudaEvent_t mid = nullptr);

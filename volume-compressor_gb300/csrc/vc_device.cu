@@ -214,6 +214,11 @@ extern "C" __attribute__((visibility("default"))) void vcg_set_rc_scalar_warps(i
     const uint32_t v = w < 0 ? vcg::kRcScalarWarpsDefault : (uint32_t)(w > 64 ? 64 : w);
     __atomic_store_n(&g_rc_scalar_warps, v, __ATOMIC_RELAXED);
 }
+static uint32_t g_rc_solo = vcg::kRcSoloDefault;
+uint32_t vcg::rc_solo_atoms() { return __atomic_load_n(&g_rc_solo, __ATOMIC_RELAXED); }
+extern "C" __attribute__((visibility("default"))) void vcg_set_rc_solo(int n) {
+    __atomic_store_n(&g_rc_solo, n < 0 ? vcg::kRcSoloDefault : (uint32_t)n, __ATOMIC_RELAXED);
+}
 
 // ---------------------------------------------------------------- allocation-failure injection
 // g_fail_alloc > 0: allocations left before one fails; -1: that failure
@@ -783,6 +788,15 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
     }
     StageEvents ev;
     memcpy(ev.ev, c->ev, sizeof ev.ev);
+    // the per-lane decoder's solo atoms run on the second stream; the slab
+    // events serve as its fork and join (the copy-out slabs record them again
+    // only after the range decode)
+    const bool solo = p_ord && rc_solo_for(n, (uint32_t)g_dev.num_sms) && vcd_side_stream(c);
+    if (solo) {
+        ev.side = c->copy_stream;
+        ev.fork = c->chunk_ev[0];
+        ev.join = c->chunk_ev[1];
+    }
     uint64_t ctl_h[2] = {0xFFFFFFFFull, 0};
     // Large outputs to pinned host memory: the inverse transform runs in up to 32
     // slabs of atom layers and each finished slab is copied out on a second stream while
@@ -885,7 +899,7 @@ static int decode_job(vcd_ctx *c, const uint8_t *arc, const vcd_atom *atoms, uin
                          n);
         } else {
             // (the per-lane decoder: length sort in three kernels, then the decoder)
-            vcd_prof_add("rc_decode", vcd_elapsed(ev.ev[1], ev.ev[2]), n ? (p_ord ? 4 : 1) : 0,
+            vcd_prof_add("rc_decode", vcd_elapsed(ev.ev[1], ev.ev[2]), n ? (p_ord ? (solo ? 6 : 4) : 1) : 0,
                          r->payload_bytes + 16 * n, 4 * nnz, r->present);
             vcd_prof_add("idct", vcd_elapsed(ev.ev[2], ev.ev[3]), n ? 1 : 0, 4 * nnz + 16 * n, out_bytes, n);
         }

@@ -25,7 +25,7 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_mark_zero_region", "vc_writer_decode_atom", "vc_writer_coverage", "vc_writer_decode_2x2x2",
               "vc_writer_close"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps", "vcg_set_rc_solo",
                "vcg_set_stream_threads", "vcg_memory_read", "vcg_downscale2x", "vcg_downscale_pyramid",
                "vcg_append_atom_async", "vcg_writer_flush",
                "vcg_encode_ds", "vcg_dct_forward", "vcg_dct_inverse",
@@ -200,6 +200,7 @@ def lib():
         L.vcg_set_batch_shape.argtypes = [ctypes.c_int] * 3
         L.vcg_repack_v2.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_size_t)]
         L.vcg_set_rc_scalar_warps.argtypes = [ctypes.c_int]
+        L.vcg_set_rc_solo.argtypes = [ctypes.c_int]
         L.vcg_dct_forward.argtypes = [P, Dims, ctypes.c_int, ctypes.c_int, P, P, ctypes.POINTER(ctypes.c_uint32)]
         L.vcg_dct_inverse.argtypes = [P, P, Dims, ctypes.c_int, ctypes.c_int, P, ctypes.POINTER(ctypes.c_uint32)]
         L.vcg_server_create.restype = P
