@@ -1,11 +1,13 @@
-"""The per-lane range decoder (every lane of a warp decodes its own atom, atoms
-ordered by payload length) takes every decode of more than a few thousand
-atoms. Here it is forced on for every decode (range-decoder policy 0) and must
-give the reference's bits on the stored golden archives, and the oracle's
-statuses and bytes on corrupt and truncated ones, including a stream with an
-over-long escape prefix (malformed: VC_ERR_FORMAT). Every case runs with no
-solo atoms, with the 3 longest atoms on latency-decoder warps of their own,
-and with every atom on one."""
+"""Range-decoder policy 0 (no atom gets a warp of its own): decodes of up to
+608 atoms (one per SM sub-partition: all the stored golden archives) run the
+warp-lockstep decoder, several atoms per warp walking the scan positions
+together; larger ones run the per-lane decoder (every lane of a warp its own
+atom, atoms ordered by payload length), which the full-size archives of
+test_gpu_encode exercise and the host build of test_host_decoders checks
+stream by stream. Here the lockstep decoder must give the reference's bits on
+the stored golden archives, and the oracle's statuses and bytes on corrupt and
+truncated ones, including a stream with an over-long escape prefix
+(malformed: VC_ERR_FORMAT)."""
 import hashlib
 import struct
 
@@ -23,17 +25,15 @@ def sha(b):
     return hashlib.sha256(bytes(b)).hexdigest()
 
 
-@pytest.fixture(params=[0, 3, 1 << 30], ids=["solo0", "solo3", "solo_all"])
-def lanes(vc, gpu, request):
+@pytest.fixture
+def lockstep(vc, gpu):
     vc.lib().vcg_set_rc_scalar_warps(0)
-    vc.lib().vcg_set_rc_solo(request.param)
     yield
     vc.lib().vcg_set_rc_scalar_warps(-1)
-    vc.lib().vcg_set_rc_solo(-1)
 
 
 @pytest.mark.parametrize("name", STORED)
-def test_lane_decoder_matches_reference(vc, golden, lanes, name):
+def test_lockstep_decoder_matches_reference(vc, golden, lockstep, name):
     c = golden[name]
     a = vc.Archive(load_archive(c))
     for lod, h in enumerate(c["lod_sha256"]):
@@ -44,7 +44,7 @@ def test_lane_decoder_matches_reference(vc, golden, lanes, name):
         assert s == r["status"] and sha(out) == r["sha256"]
 
 
-def test_lane_decoder_corrupt_payloads_match_oracle(vc, oracle, golden, lanes):
+def test_lockstep_decoder_corrupt_payloads_match_oracle(vc, oracle, golden, lockstep):
     base = bytearray(load_archive(golden["synth_prime_97x131x65_t20"]))
     rng = np.random.default_rng(2024)
     atoms = [(0, 0, 0), (1, 2, 1), (0, 3, 2), (1, 0, 3)]
@@ -68,7 +68,7 @@ def test_lane_decoder_corrupt_payloads_match_oracle(vc, oracle, golden, lanes):
                 assert (g == r).all(), (trial, lod)
 
 
-def test_lane_decoder_rejects_overlong_escape(vc, oracle, golden, lanes):
+def test_lockstep_decoder_rejects_overlong_escape(vc, oracle, golden, lockstep):
     """An atom whose payload is replaced (in place, same length budget) by a
     stream with a 40-one escape prefix: the oracle and the GPU report
     VC_ERR_FORMAT for the LOD and for that atom, and decode the atoms before it
@@ -94,7 +94,7 @@ def test_lane_decoder_rejects_overlong_escape(vc, oracle, golden, lanes):
     assert s1 == s2 == vc.VC_ERR_FORMAT and (at == 0).all() and (at2 == 0).all()
 
 
-def test_lane_decoder_truncated_archive_matches_oracle(vc, oracle, golden, lanes):
+def test_lockstep_decoder_truncated_archive_matches_oracle(vc, oracle, golden, lockstep):
     data = load_archive(golden["synth_prime_97x131x65_t20"])
     for cut in [len(data) - 1, len(data) - 3000, 650000]:
         d = data[:cut]

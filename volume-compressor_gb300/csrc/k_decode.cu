@@ -355,7 +355,8 @@ static void launch_rc(const DecodeJob &J, int num_sms, cudaStream_t s, const Sta
             Jl.order = J.order + ns;
             Jl.sort_ctl = J.sort_ctl + 2;   // Jl.sort_ctl[kSortBuckets]: the per-lane count
         }
-        k_rc_lanes<<<(unsigned)((J.n_atoms - ns + kLaneThreads - 1) / kLaneThreads), kLaneThreads, 0, s>>>(Jl);
+        const uint64_t lane_blocks = (J.n_atoms - ns + kLaneThreads - 1) / kLaneThreads;
+        if (lane_blocks) k_rc_lanes<<<(unsigned)lane_blocks, kLaneThreads, 0, s>>>(Jl);   // (0: every atom solo)
         if (ns) cudaStreamWaitEvent(s, ev->join, 0);
         return;
     }
