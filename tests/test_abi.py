@@ -119,3 +119,48 @@ def test_argument_validation_needs_no_device(vc, golden):
         s = L.vc_encode(vc.ptr(vol), vc.Dims(*dims), ctypes.c_float(t), ctypes.byref(out), ctypes.byref(n))
         assert s == vc.VC_ERR_RANGE
     assert L.vc_region_atoms() == 32
+
+
+@pytest.mark.parametrize("name", ["synth_prime_97x131x65_t20", "ref_test_basic", "synth_flat_96x64x33_t100", "tiny_1x1x1"])
+def test_request_validation_matches_oracle(vc, oracle, golden, name):
+    """Every region, atom and LOD request the oracle rejects as out of range
+    (src/vc/vc.c:1404-1421, 1535-1555: LOD outside the archive, atom outside
+    the LOD, empty box, box past the LOD's edge) is rejected by the library
+    with VC_ERR_RANGE before it needs a device, and no other: with no device a
+    request the oracle accepts gets VC_ERR_IO (on a GPU it would be decoded)."""
+    data = load_archive(golden[name])
+    a, o = vc.Archive(data), oracle.Archive(data)
+    rng = np.random.default_rng(0xA46)
+    edge = [0, 1, 2, 31, 32, 33, 63, 64, 96, 97, 98, 130, 131, 132, 2047, 2048, 2049, 0xFFFFFFFF, 0x80000000]
+
+    def coord(hi):
+        return int(rng.choice(edge)) if rng.integers(0, 3) == 0 else int(rng.integers(0, hi + 3))
+
+    ranged = accepted = 0
+    for _ in range(400):
+        lod = int(rng.choice([-1, 0, 0, 1, 2, o.nlod - 1, o.nlod, 8, 9]))
+        s, dims = o.lod_dims(lod) if 0 <= lod < o.nlod else (0, (4, 4, 4))
+        lo, hi = [], []
+        for d in dims:   # a valid extent on most axes, edge and random values on the others
+            if rng.integers(0, 100) < 85:
+                x0 = int(rng.integers(0, d))
+                lo.append(x0)
+                hi.append(int(rng.integers(x0 + 1, d + 1)))
+            else:
+                lo.append(coord(d))
+                hi.append(coord(d))
+        box = (lo[0], lo[1], lo[2], hi[0], hi[1], hi[2])
+        n = (box[3] - box[0]) * (box[4] - box[1]) * (box[5] - box[2]) if box[3] > box[0] and box[4] > box[1] \
+            and box[5] > box[2] else 0
+        # a box larger than the whole LOD cannot be valid: both must refuse it before writing
+        out = np.zeros(n if 0 < n <= dims[0] * dims[1] * dims[2] else 1, np.uint8)
+        so = oracle.lib().orc_decode_region(o.h, lod, oracle.Box(*box), out.ctypes.data)
+        sa = vc.lib().vc_decode_region(a.h, lod, vc.Box(*box), out.ctypes.data)
+        assert (sa == vc.VC_ERR_RANGE) == (so == vc.VC_ERR_RANGE), (lod, box, sa, so)
+        ranged += so == vc.VC_ERR_RANGE
+        accepted += so != vc.VC_ERR_RANGE
+        ax, ay, az = (coord((d + 31) // 32) for d in dims)
+        s1, _ = a.decode_atom(lod, ax, ay, az)
+        s2, _ = o.decode_atom(lod, ax, ay, az)
+        assert (s1 == vc.VC_ERR_RANGE) == (s2 == vc.VC_ERR_RANGE), (lod, ax, ay, az, s1, s2)
+    assert ranged > 50 and accepted > 20
