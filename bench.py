@@ -535,8 +535,8 @@ def config4_batched(n_boxes=10000, plain_sample=100, batch_repeats=3):
             "batched_ms": batch_ms, "batched_GBps": batch_gbps, "batched_us_per_request": batch_ms * 1e3 / n_boxes,
             "plain_GBps": plain_gbps, "plain_p50_us": plain_ms[len(plain_ms) // 2] * 1e3,
             "plain_p99_us": plain_ms[min(len(plain_ms) - 1, int(0.99 * len(plain_ms)))] * 1e3,
-            "speedup_vs_plain": batch_gbps / plain_gbps, "candidates_ms": cand, "autotuned_shape": {"rc_scalar_warps": shape[0], "transform_imma": shape[2],
-                                                                            "transform_threads": shape[1]},
+            "speedup_vs_plain": batch_gbps / plain_gbps, "candidates_ms": cand,
+            "autotuned_shape": {"rc_scalar_warps": shape[0], "transform_imma": shape[2], "transform_threads": shape[1]},
             "bit_exact_sample": ok, "plain_sample": plain_sample,
             "bit_exact_vs_reference": {"archive": arc_ok, "boxes": ref_ok, "boxes_checked": ref_n},
             "cpu_baseline": cpu}

@@ -121,7 +121,8 @@ def test_argument_validation_needs_no_device(vc, golden):
     assert L.vc_region_atoms() == 32
 
 
-@pytest.mark.parametrize("name", ["synth_prime_97x131x65_t20", "ref_test_basic", "synth_flat_96x64x33_t100", "tiny_1x1x1"])
+@pytest.mark.parametrize("name", ["synth_prime_97x131x65_t20", "ref_test_basic", "synth_flat_96x64x33_t100",
+                                  "tiny_1x1x1"])
 def test_request_validation_matches_oracle(vc, oracle, golden, name):
     """Every region, atom and LOD request the oracle rejects as out of range
     (src/vc/vc.c:1404-1421, 1535-1555: LOD outside the archive, atom outside

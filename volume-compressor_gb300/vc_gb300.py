@@ -25,14 +25,16 @@ VC_SYMBOLS = ["vc_encode", "vc_open", "vc_close", "vc_lod_dims", "vc_decode_lod"
               "vc_mark_zero_region", "vc_writer_decode_atom", "vc_writer_coverage", "vc_writer_decode_2x2x2",
               "vc_writer_close"]
 VCG_SYMBOLS = ["vcg_decode_region_device", "vcg_decode_lod_device", "vcg_make_resident", "vcg_encode_device",
-               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape", "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps", "vcg_set_rc_solo",
+               "vcg_encode_q", "vcg_decode_atoms_noalloc", "vcg_decode_regions", "vcg_batch_shape",
+               "vcg_set_batch_shape", "vcg_repack_v2", "vcg_set_rc_scalar_warps", "vcg_set_rc_solo",
                "vcg_set_stream_threads", "vcg_memory_read", "vcg_downscale2x", "vcg_downscale_pyramid",
                "vcg_append_atom_async", "vcg_writer_flush",
                "vcg_encode_ds", "vcg_dct_forward", "vcg_dct_inverse",
                "vcg_server_create", "vcg_server_submit", "vcg_server_wait", "vcg_server_stats",
                "vcg_server_destroy",
                "vcg_synth_volume_device", "vcg_alloc", "vcg_free", "vcg_alloc_host", "vcg_free_host", "vcg_copy",
-               "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_device_memory", "vcg_debug_fail_alloc", "vcg_last_error", "vcg_profile_enable",
+               "vcg_memset", "vcg_sync", "vcg_device_info", "vcg_device_memory", "vcg_debug_fail_alloc",
+               "vcg_last_error", "vcg_profile_enable",
                "vcg_profile_read", "vcg_last_call_ms"]
 
 
