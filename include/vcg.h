@@ -53,9 +53,10 @@ vc_status vcg_set_batch_shape(int rc_scalar_warps, int transform_threads, int tr
 // latency-tuned scalar decoder; up to w warps per sub-partition, one atom per
 // warp with the plain scalar decoder, longest payloads first; above that the
 // per-lane decoder (every lane of a warp decodes its own atom, atoms in order
-// of payload length). w = 0: always the per-lane decoder; w < 0 restores the
-// default (8: measured on GB300, the per-lane decoder wins from 3,000-5,000
-// atoms on, depending on the atoms' sizes).
+// of payload length). w = 0: no atom keeps a warp to itself (above one atom
+// per sub-partition the per-lane decoder, below it atoms share warps in
+// lockstep); w < 0 restores the default (8: measured on GB300, the per-lane
+// decoder wins from 3,000-5,000 atoms on, depending on the atoms' sizes).
 void vcg_set_rc_scalar_warps(int w);
 // The per-lane decoder's n longest atoms (by payload length) each get a warp of
 // their own running the latency-tuned decoder, on a second stream beside it
