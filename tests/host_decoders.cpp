@@ -86,8 +86,8 @@ int main(int argc, char **argv) {
     if (fread(&n, 4, 1, f) != 1) return 2;
     uint32_t bs[9];
     band_table(bs);
-    const char *names[6] = {"latency", "staged", "scalar", "lockstep", "per-lane", "zero-runs"};
-    int diff[6] = {0, 0, 0, 0, 0, 0};
+    const char *names[5] = {"latency", "staged", "scalar", "lockstep", "per-lane"};
+    int diff[5] = {0, 0, 0, 0, 0};
     for (uint32_t k = 0; k < n; ++k) {
         uint32_t h[3];
         if (fread(h, 4, 3, f) != 3) return 2;
@@ -98,14 +98,13 @@ int main(int argc, char **argv) {
         if (len && fread(src, 1, len, f) != len) return 2;
         std::vector<uint32_t> want(nent);
         if (nent && fread(want.data(), 4, nent, f) != nent) return 2;
-        Result r[6];
+        Result r[5];
         for (auto &x : r) x.ent.reserve(nent + 16);
         auto sink_to = [](Result &x) { return [&x](uint32_t p, uint32_t lv) { x.ent.push_back(p | (lv << 16)); }; };
         r[0].bad = rc_decode_levels_lat(src, len, bs, sink_to(r[0]));
         r[1].bad = rc_decode_levels_sm(src, len, bs, sink_to(r[1]));   // src[len] is a zero guard byte
         r[2].bad = rc_decode_levels_lane(src, len, bs, sink_to(r[2]));
         r[3].bad = rc_decode_levels_warp(src, len, true, bs, sink_to(r[3]));
-        r[5].bad = rc_decode_levels_run4(src, len, bs, sink_to(r[5]));   // src[len] is a zero guard byte
         {
             const uint32_t cap = 65536;   // more than any stream's levels (at most 32768)
             std::vector<uint32_t> dst(cap);
@@ -117,9 +116,9 @@ int main(int argc, char **argv) {
             r[4].bad = (int)L.bad;
             r[4].ent.assign(dst.begin(), dst.begin() + (L.n < cap ? L.n : cap));
         }
-        for (int d = 0; d < 6; ++d) diff[d] += !same(r[d], bad, want.data(), nent);
+        for (int d = 0; d < 5; ++d) diff[d] += !same(r[d], bad, want.data(), nent);
     }
     fclose(f);
-    for (int d = 0; d < 6; ++d) printf("%s %d %u\n", names[d], diff[d], n);
+    for (int d = 0; d < 5; ++d) printf("%s %d %u\n", names[d], diff[d], n);
     return 0;
 }

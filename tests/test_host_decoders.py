@@ -77,7 +77,7 @@ def test_golden_archive_streams(harness, oracle, golden, tmp_path):
         streams += atom_streams(oracle, load_archive(golden[name]))
     assert len(streams) > 300
     assert run(harness, oracle, streams, tmp_path) == dict.fromkeys(
-        ("latency", "staged", "scalar", "lockstep", "per-lane", "zero-runs"), 0)
+        ("latency", "staged", "scalar", "lockstep", "per-lane"), 0)
 
 
 def test_noise_escapes_truncation_and_random_streams(harness, oracle, tmp_path):
@@ -98,4 +98,4 @@ def test_noise_escapes_truncation_and_random_streams(harness, oracle, tmp_path):
     bad = [expected(oracle, s)[0] for s in streams]
     assert sum(bad) >= 2 and sum(bad) < len(streams)
     assert run(harness, oracle, streams, tmp_path) == dict.fromkeys(
-        ("latency", "staged", "scalar", "lockstep", "per-lane", "zero-runs"), 0)
+        ("latency", "staged", "scalar", "lockstep", "per-lane"), 0)

@@ -652,114 +652,6 @@ __device__ __forceinline__ int rc_decode_levels_sm(const uint8_t *s, uint32_t le
     return 0;
 }
 
-// ---------------------------------------------------------------- latency decoder, zero runs
-// The staged latency decoder with the significance decisions taken up to four
-// at a time. While the decisions are zeros (no level at the position) the code
-// word does not change and the band's probability moves by a fixed rule, so the
-// splits of the next four decisions, each assuming that the ones before it were
-// zeros, form a short chain (a high multiply and a renormalisation shift per
-// decision) whose comparisons with the code lie off the chain. The zeros before
-// the first one (or the band's end) are committed at once; a one goes on as a
-// single decision. Same results as rc_decode_levels_sm (checked on the host
-// against the oracle, stream by stream); no kernel runs it until it has been
-// timed against rc_decode_levels_sm on the GPU.
-
-// stream byte q (0 past the end: s[len] == 0)
-__device__ __forceinline__ uint32_t rcs_byte(const RcSm &in, uint32_t q) { return in.s[q < in.len ? q : in.len]; }
-
-// the window after b more bytes (1..4) of the stream have entered the code
-__device__ __forceinline__ void rcs_skip(RcSm &in, uint32_t b) {
-    const uint32_t q = in.pos + 4u;
-    const uint32_t nw = (rcs_byte(in, q) << 24) | (rcs_byte(in, q + 1u) << 16) | (rcs_byte(in, q + 2u) << 8) |
-                        rcs_byte(in, q + 3u);
-    in.w = b >= 4u ? nw : rcs_fsl(nw, in.w, 8u * b);
-    in.pos += b;
-}
-
-// s: the stream in shared memory, s[len] == 0
-template <class Sink>
-__device__ __forceinline__ int rc_decode_levels_run4(const uint8_t *s, uint32_t len, const uint32_t *band_start,
-                                                     Sink &&sink) {
-    RcSm in;
-    in.s = s;
-    in.len = len;
-    uint32_t code = 0;
-#pragma unroll
-    for (uint32_t i = 0; i < 5; ++i) code = (code << 8) | s[i < len ? i : len];
-    in.pos = 5;
-    in.w = 0;
-#pragma unroll
-    for (uint32_t i = 5; i < 9; ++i) in.w = (in.w << 8) | s[i < len ? i : len];
-    uint32_t range = 0xFFFFFFFFu, eob = 0;
-#pragma unroll
-    for (int i = 0; i < 16; ++i) eob = (eob << 1) | (rcs_bypass(code, range, in) ? 0u : 1u);
-    if (eob > 32768u) eob = 32768u;   // src/vc/vc.c:549
-    uint32_t mag[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) mag[k] = 2048u;
-    for (int bnd = 0; bnd < 8; ++bnd) {
-        uint32_t p = band_start[bnd];
-        if (p >= eob) break;
-        const uint32_t lim = band_start[bnd + 1] < eob ? band_start[bnd + 1] : eob;
-        uint32_t sig = 2048u;
-        while (p < lim) {
-            const uint32_t n = lim - p < 4u ? lim - p : 4u;   // decisions this block may take
-            // decision j's split and the state before it, if decisions 0..j-1 were zeros
-            const uint32_t P0 = sig, R0 = range;
-            const uint32_t r00 = __umulhi(R0, P0 << 20), s0 = rcs_clz(r00) & 8u;
-            const uint32_t P1 = P0 - (uint32_t)((int32_t)(P0 - 4065u) >> 5), R1 = r00 << s0;
-            const uint32_t r01 = __umulhi(R1, P1 << 20), s1 = rcs_clz(r01) & 8u;
-            const uint32_t P2 = P1 - (uint32_t)((int32_t)(P1 - 4065u) >> 5), R2 = r01 << s1;
-            const uint32_t r02 = __umulhi(R2, P2 << 20), s2 = rcs_clz(r02) & 8u;
-            const uint32_t P3 = P2 - (uint32_t)((int32_t)(P2 - 4065u) >> 5), R3 = r02 << s2;
-            const uint32_t r03 = __umulhi(R3, P3 << 20), s3 = rcs_clz(r03) & 8u;
-            const uint32_t P4 = P3 - (uint32_t)((int32_t)(P3 - 4065u) >> 5), R4 = r03 << s3;
-            const uint32_t S1 = s0, S2 = S1 + s1, S3 = S2 + s2, S4 = S3 + s3;   // code bits shifted in
-            const uint32_t C1 = rcs_fsl(in.w, code, S1), C2 = rcs_fsl(in.w, code, S2), C3 = rcs_fsl(in.w, code, S3);
-            uint32_t m = n;   // the first one among the block's decisions (n: none)
-            if (n > 3u && C3 >= r03) m = 3u;
-            if (n > 2u && C2 >= r02) m = 2u;
-            if (n > 1u && C1 >= r01) m = 1u;
-            if (code >= r00) m = 0u;
-            // commit the m zeros
-            const uint32_t Sm = m == 0u ? 0u : m == 1u ? S1 : m == 2u ? S2 : m == 3u ? S3 : S4;
-            const uint32_t Cm = m == 0u ? code : m == 1u ? C1 : m == 2u ? C2 : m == 3u ? C3
-                                : S4 >= 32u ? in.w : rcs_fsl(in.w, code, S4);
-            range = m == 0u ? R0 : m == 1u ? R1 : m == 2u ? R2 : m == 3u ? R3 : R4;
-            sig = m == 0u ? P0 : m == 1u ? P1 : m == 2u ? P2 : m == 3u ? P3 : P4;
-            code = Cm;
-            if (Sm) rcs_skip(in, Sm >> 3);
-            p += m;
-            if (m == n) continue;   // all zeros
-            // decision m is a one: a level at p
-            const uint32_t r0 = m == 0u ? r00 : m == 1u ? r01 : m == 2u ? r02 : r03;
-            sig = sig - (sig >> 5);
-            rcs_norm(code, range, code - r0, range - r0, in);
-            uint32_t v = 0;   // unary magnitude, then EG0 escape (src/vc/vc.c:491-506)
-#pragma unroll
-            for (int k = 0; k < 12; ++k) {
-                if (rcs_bit(code, range, mag[k], in)) {
-                    v = (uint32_t)k + 1u;
-                    break;
-                }
-            }
-            if (v == 0) {
-                uint32_t ones = 0;
-                while (!rcs_bypass(code, range, in)) {
-                    if (++ones > 32u) return 1;
-                }
-                uint32_t x = 1;
-                for (uint32_t i = 0; i < ones; ++i) x = (x << 1) | (rcs_bypass(code, range, in) ? 0u : 1u);
-                v = 11u + x;
-            }
-            const bool neg = !rcs_bypass(code, range, in);
-            sink(p, (neg ? 0u - v : v) & 0xFFFFu);
-            ++p;
-        }
-    }
-    return 0;
-}
-
 // ---------------------------------------------------------------- encoder
 // WRITE = false only tracks the interval width: the byte count of the
 // reference encoder equals its number of shift-low calls (renormalisation
