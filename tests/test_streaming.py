@@ -230,6 +230,54 @@ def test_host_lookups_streaming(vc, golden, name, ver):
         o.close()
 
 
+@pytest.mark.parametrize("ver", [1, 2])
+def test_host_lookups_streaming_random_failed_reads(vc, golden, ver):
+    """Reads failing over random byte ranges (1 to 5 ranges of 1 to 64 bytes,
+    anywhere in the file: header, index, slots or payloads): the library's
+    streaming archive opens exactly when the oracle's does and resolves every
+    atom to the same payload range (host code only, no decode)."""
+    rng = np.random.default_rng(0x57E + ver)
+    opened = differs = 0
+    for name in CASES:
+        data = archive_bytes(golden, name, ver)
+        clean = O.StreamingArchive(Poisoned(data), len(data))
+        ref = {(lod, a): clean.payload_range(lod, *a) for lod in range(clean.nlod)
+               for a in atoms(clean.lod_dims(lod)[1])}
+        clean.close()
+        keys = sorted(k for k, v in ref.items() if v[0] == 2)   # PRESENT atoms: their regions are indexed
+        for _ in range(12):
+            ranges = []
+            for _ in range(int(rng.integers(1, 6))):
+                if rng.integers(0, 2):   # anywhere
+                    lo = int(rng.integers(0, len(data)))
+                    ranges.append((lo, lo + int(rng.integers(1, 65))))
+                    continue
+                lod, (az, ay, ax) = keys[int(rng.integers(0, len(keys)))]   # a used slot or index entry
+                if rng.integers(0, 2):
+                    lo = slot_offset(data, lod, az, ay, ax) + int(rng.integers(0, 16))
+                elif ver == 1:
+                    lo = l1_bucket(data, lod, az // 32, ay // 32, ax // 32) + int(rng.integers(0, 16))
+                else:
+                    lo = dir_entry(data, lod, az // 32, ay // 32, ax // 32) + int(rng.integers(0, 16))
+                ranges.append((lo, lo + 1))
+            a = vc.StreamingArchive(Poisoned(data, ranges), len(data))
+            o = O.StreamingArchive(Poisoned(data, ranges), len(data))
+            assert bool(a) == bool(o.h), (name, ranges)
+            if not a:
+                continue
+            opened += 1
+            for lod in range(o.nlod):
+                s, dims = a.lod_dims(lod)
+                assert (s, dims) == o.lod_dims(lod)
+                for at in atoms(dims):
+                    pr = a.payload_range(lod, *at)
+                    assert pr == o.payload_range(lod, *at), (name, ranges, lod, at)
+                    differs += pr != ref[(lod, at)]
+            a.close()
+            o.close()
+    assert opened >= 20 and differs > 0
+
+
 def blob(vc, a, lod, rz, ry, rx):
     import ctypes
     off, ln = ctypes.c_uint64(), ctypes.c_uint64()
