@@ -136,3 +136,38 @@ def test_gpu_concurrent_appends_decode_like_canonical(vc, gpu, golden, tmp_path,
         assert s == 0 and hashlib.sha256(out.tobytes()).hexdigest() == want, lod
     ref = load_archive(g)
     assert abs(len(data) - len(ref)) < 16 * 32768 * 16   # same payloads, blocks in another order
+
+
+def test_random_marks_sessions_match_reference(vc):
+    """Random writer sessions of zero marks, base_q settings and coverage
+    queries (odd and large dims, coordinates in and past every LOD, repeated
+    and overlapping marks, q outside the clamp range), no atom contents, run
+    live on the reference's own writer (oracle/_ref, built on this host only)
+    and on this library: every op's result and the closed file's bytes are the
+    reference's."""
+    import refcodec
+    if not refcodec.available():
+        pytest.skip("reference build (oracle/_ref) not present on this host")
+    R = W.bind(refcodec.lib())
+    L = mylib(vc)
+    rng = np.random.default_rng(0x3A4C)
+    for trial in range(24):
+        dims = [int(rng.choice([1, 31, 32, 33, 97, 300, 1024, 2100, 4097])) for _ in range(3)]
+        ops = [["create", dims, float(rng.choice([1.0, 12.0, 100.0]))]]
+        for _ in range(int(rng.integers(5, 60))):
+            lod = int(rng.choice([0, 0, 1, 2, 3, 7, 8, -1]))
+            d = [max(1, (v + (1 << max(lod, 0)) - 1) >> max(lod, 0)) for v in dims]
+            at = [int(rng.integers(0, (v + 31) // 32 + 2)) for v in d]   # x, y, z atoms, a few past the edge
+            rg = [int(rng.integers(0, (v + 1023) // 1024 + 2)) for v in d]
+            k = int(rng.integers(0, 10))
+            if k < 4:
+                ops.append(["zatom", lod, at[2], at[1], at[0]])
+            elif k < 5:
+                ops.append(["zregion", lod, rg[2], rg[1], rg[0]])
+            elif k < 6:
+                ops.append(["q", lod, float(rng.choice([0.001, 0.05, 1.5, 4096.0, 9000.0]))])
+            else:
+                ops.append(["cov", lod, at[2], at[1], at[0]])
+        ops.append(["close"])
+        s = {"volume": [[8, 8, 8], 1], "ops": ops}
+        assert W.run(L, s, vc.synth) == W.run(R, s, vc.synth), trial
