@@ -7,7 +7,9 @@ into another table entry), random slot bytes, region keys overwritten, header
 counters changed, v2 headers and directories hit, and truncations. Every
 archive must open or fail to open on both, and then give the same LOD
 dimensions and, for every atom (and one past each edge), the same coverage and
-payload range."""
+payload range. Where the reference's own build exists (oracle/_ref, this host
+only) the oracle's answers are also checked against the reference's reader
+on the same damaged archives, which pins the oracle there."""
 import json
 import lzma
 import os
@@ -54,6 +56,40 @@ def mismatch(vc, oracle, data):
     return None
 
 
+def reference_mismatch(oracle, data):
+    """The oracle against the reference's reader (None: same answers)."""
+    import ctypes
+    import refcodec
+    L = refcodec.lib()
+    L.vc_atom_payload_range.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64),
+                                        ctypes.POINTER(ctypes.c_uint32)]
+    o, r = oracle.Archive(data), refcodec.RefArchive(data)
+    try:
+        if bool(o.h) != bool(r.h):
+            return ("open", bool(o.h), bool(r.h))
+        if not o.h:
+            return None
+        for lod in range(o.nlod + 1):
+            s, (nx, ny, nz) = o.lod_dims(lod)
+            if r.lod_dims(lod) != (s, (nx, ny, nz)):
+                return ("dims", lod)
+            if s:
+                continue
+            for az in range((nz + 31) // 32 + 1):
+                for ay in range((ny + 31) // 32 + 1):
+                    for ax in range((nx + 31) // 32 + 1):
+                        off, ln = ctypes.c_uint64(), ctypes.c_uint32()
+                        c = L.vc_atom_payload_range(r.h, lod, az, ay, ax, ctypes.byref(off), ctypes.byref(ln))
+                        if (o.coverage(lod, az, ay, ax) != r.coverage(lod, az, ay, ax) or
+                                o.payload_range(lod, az, ay, ax) != (c, off.value, ln.value)):
+                            return ("atom", lod, az, ay, ax)
+        return None
+    finally:
+        o.close()
+        r.close()
+
+
 def corrupt_v1(rng, base, trial):
     l1_cap, _, l1_off = struct.unpack_from("<QQQ", base, 40)
     d = bytearray(base)
@@ -92,6 +128,8 @@ def corrupt_v2(rng, base, trial):
 
 @pytest.mark.parametrize("seed", [1, 2])
 def test_damaged_metadata_resolves_like_oracle(vc, oracle, golden, seed):
+    import refcodec
+    with_ref = refcodec.available()
     rng = np.random.default_rng(seed)
     cases = [(load_archive(golden[n]), corrupt_v1, 60) for n in V1]
     for c in json.load(open(os.path.join(GOLDEN, "v2.json")))["cases"]:
@@ -105,6 +143,9 @@ def test_damaged_metadata_resolves_like_oracle(vc, oracle, golden, seed):
             d = corrupt(rng, base, trial)
             bad = mismatch(vc, oracle, d)
             assert bad is None, (trial, bad)
+            if with_ref:
+                bad = reference_mismatch(oracle, d)
+                assert bad is None, ("oracle against the reference", trial, bad)
             o = oracle.Archive(d)
             changed += not o.h or atom_table(o) != clean
             n += 1
