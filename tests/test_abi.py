@@ -128,9 +128,12 @@ def test_request_validation_matches_oracle(vc, oracle, golden, name):
     (src/vc/vc.c:1404-1421, 1535-1555: LOD outside the archive, atom outside
     the LOD, empty box, box past the LOD's edge) is rejected by the library
     with VC_ERR_RANGE before it needs a device, and no other: with no device a
-    request the oracle accepts gets VC_ERR_IO (on a GPU it would be decoded)."""
+    request the oracle accepts gets VC_ERR_IO (on a GPU it would be decoded).
+    Where the reference's build exists, its answers equal the oracle's."""
+    import refcodec
     data = load_archive(golden[name])
     a, o = vc.Archive(data), oracle.Archive(data)
+    r = refcodec.RefArchive(data) if refcodec.available() else None   # the reference's own build, this host only
     rng = np.random.default_rng(0xA46)
     edge = [0, 1, 2, 31, 32, 33, 63, 64, 96, 97, 98, 130, 131, 132, 2047, 2048, 2049, 0xFFFFFFFF, 0x80000000]
 
@@ -158,10 +161,16 @@ def test_request_validation_matches_oracle(vc, oracle, golden, name):
         so = oracle.lib().orc_decode_region(o.h, lod, oracle.Box(*box), out.ctypes.data)
         sa = vc.lib().vc_decode_region(a.h, lod, vc.Box(*box), out.ctypes.data)
         assert (sa == vc.VC_ERR_RANGE) == (so == vc.VC_ERR_RANGE), (lod, box, sa, so)
+        if r is not None:
+            sr = refcodec.lib().vc_decode_region(r.h, lod, refcodec.Box(*box), out.ctypes.data)
+            assert (sr == vc.VC_ERR_RANGE) == (so == vc.VC_ERR_RANGE), ("oracle against the reference", lod, box)
         ranged += so == vc.VC_ERR_RANGE
         accepted += so != vc.VC_ERR_RANGE
         ax, ay, az = (coord((d + 31) // 32) for d in dims)
         s1, _ = a.decode_atom(lod, ax, ay, az)
         s2, _ = o.decode_atom(lod, ax, ay, az)
         assert (s1 == vc.VC_ERR_RANGE) == (s2 == vc.VC_ERR_RANGE), (lod, ax, ay, az, s1, s2)
+        if r is not None:
+            s3, _ = r.decode_atom(lod, ax, ay, az)
+            assert (s3 == vc.VC_ERR_RANGE) == (s2 == vc.VC_ERR_RANGE), ("oracle against the reference", lod, ax, ay, az)
     assert ranged > 50 and accepted > 20
