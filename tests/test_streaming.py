@@ -235,7 +235,11 @@ def test_host_lookups_streaming_random_failed_reads(vc, golden, ver):
     """Reads failing over random byte ranges (1 to 5 ranges of 1 to 64 bytes,
     anywhere in the file: header, index, slots or payloads): the library's
     streaming archive opens exactly when the oracle's does and resolves every
-    atom to the same payload range (host code only, no decode)."""
+    atom to the same payload range (host code only, no decode). Where the
+    reference's own build exists, its streaming reader opens the same archives
+    and gives every atom the oracle's coverage."""
+    import refcodec
+    with_ref = refcodec.available()
     rng = np.random.default_rng(0x57E + ver)
     opened = differs = 0
     for name in CASES:
@@ -263,6 +267,13 @@ def test_host_lookups_streaming_random_failed_reads(vc, golden, ver):
             a = vc.StreamingArchive(Poisoned(data, ranges), len(data))
             o = O.StreamingArchive(Poisoned(data, ranges), len(data))
             assert bool(a) == bool(o.h), (name, ranges)
+            if with_ref:
+                r = refcodec.RefStreamingArchive(Poisoned(data, ranges), len(data))
+                assert bool(r.h) == bool(o.h), ("oracle against the reference", name, ranges)
+                for lod in range(o.nlod if o.h else 0):
+                    for at in atoms(o.lod_dims(lod)[1]):
+                        assert r.coverage(lod, *at) == o.coverage(lod, *at), ("oracle against the reference", lod, at)
+                r.close()
             if not a:
                 continue
             opened += 1
