@@ -44,7 +44,7 @@ def ref_writer():
     import refcodec
     if not refcodec.available():
         pytest.skip("reference build (oracle/_ref) not present on this host")
-    return W.bind(refcodec.lib())
+    return W.bind(ctypes.CDLL(refcodec.REF_SO))   # own handle: the script's ctypes types
 
 
 def without_readback(session):

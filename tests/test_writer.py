@@ -148,7 +148,7 @@ def test_random_marks_sessions_match_reference(vc):
     import refcodec
     if not refcodec.available():
         pytest.skip("reference build (oracle/_ref) not present on this host")
-    R = W.bind(refcodec.lib())
+    R = W.bind(ctypes.CDLL(refcodec.REF_SO))   # own handle: the script's ctypes types
     L = mylib(vc)
     rng = np.random.default_rng(0x3A4C)
     for trial in range(24):
