@@ -95,11 +95,3 @@ def test_config2_1024_archives_match_reference(vc, gpu, golden, t):
     for r in c["regions"]:
         s, out = a.decode_region(r["lod"], tuple(r["box"]))
         assert s == 0 and sha(out) == r["sha256"]
-    if t == 10:   # LOD0 on the per-lane decoder with solo atoms (vcg_set_rc_solo): a few, then every atom
-        for n in (76, 1 << 30):
-            vc.lib().vcg_set_rc_solo(n)
-            try:
-                s, v = a.decode_lod(0)
-            finally:
-                vc.lib().vcg_set_rc_solo(-1)
-            assert s == 0 and sha(v) == c["lod_sha256"][0], n
