@@ -28,3 +28,21 @@ def test_server_scenarios(tmp_path):
     lines = r.stdout.strip().splitlines()
     assert r.returncode == 0, r.stdout + r.stderr
     assert len(lines) == 7 and all(line.endswith(" ok") for line in lines), r.stdout
+
+
+def test_server_scenarios_race_free(tmp_path):
+    """The same scenarios under ThreadSanitizer: no data race in the server
+    (it found one: workers read their count while vcg_server_create was still
+    raising it, which the creation now does under the server's lock)."""
+    exe = str(tmp_path / "host_server_tsan")
+    srcs = [os.path.join(ROOT, "tests", "host_server.c"),
+            os.path.join(ROOT, "volume-compressor_gb300", "csrc", "vc_server.c")]
+    r = subprocess.run(["gcc", "-O1", "-g", "-std=gnu11", "-fsanitize=thread", "-I", os.path.join(ROOT, "include"),
+                        *srcs, "-lpthread", "-o", exe], capture_output=True, text=True)
+    if r.returncode:
+        pytest.skip("no ThreadSanitizer with this compiler: " + r.stderr[-200:])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    if "FATAL: ThreadSanitizer" in r.stderr:   # e.g. an address-space layout it cannot run in
+        pytest.skip(r.stderr.strip().splitlines()[0])
+    assert "WARNING: ThreadSanitizer" not in r.stderr, r.stderr[:4000]
+    assert r.returncode == 0 and r.stdout.count(" ok") == 7, r.stdout + r.stderr[-2000:]

@@ -45,6 +45,12 @@ typedef struct vcg_server {
     uint32_t max_batch;
     int nworkers, stop;
     pthread_t th[8];
+    struct srv_worker {     // a worker's batch arrays (max_batch entries each)
+        struct vcg_server *s;
+        vcg_region_request *batch;
+        vc_status *st;
+        uint64_t *tix;
+    } w[8];
     pthread_mutex_t mu;
     pthread_cond_t work_cv, done_cv;
     srv_req *reqs;          // ticket t is reqs[t - base]
@@ -74,12 +80,13 @@ static uint64_t cost_of(const vc_box *b) {
 }
 
 static void *worker(void *arg) {
-    vcg_server *s = (vcg_server *)arg;
-    vcg_region_request *batch = (vcg_region_request *)malloc(s->max_batch * sizeof(vcg_region_request));
-    vc_status *st = (vc_status *)malloc(s->max_batch * sizeof(vc_status));
-    uint64_t *tix = (uint64_t *)malloc(s->max_batch * sizeof(uint64_t));
+    struct srv_worker *w = (struct srv_worker *)arg;
+    vcg_server *s = w->s;
+    vcg_region_request *batch = w->batch;
+    vc_status *st = w->st;
+    uint64_t *tix = w->tix;
+    pthread_mutex_lock(&s->mu);   // (held by vcg_server_create until every worker exists)
     const int big_slots = s->nworkers > 1 ? s->nworkers - 1 : 1;
-    pthread_mutex_lock(&s->mu);
     for (;;) {
         while (!s->stop && s->q_small + s->q_big == 0) pthread_cond_wait(&s->work_cv, &s->mu);
         if (s->stop && s->q_small + s->q_big == 0) break;
@@ -162,10 +169,15 @@ static void *worker(void *arg) {
         pthread_cond_broadcast(&s->work_cv);
     }
     pthread_mutex_unlock(&s->mu);
-    free(batch);
-    free(st);
-    free(tix);
     return NULL;
+}
+
+static void free_workers(vcg_server *s) {
+    for (int i = 0; i < 8; ++i) {
+        free(s->w[i].batch);
+        free(s->w[i].st);
+        free(s->w[i].tix);
+    }
 }
 
 // device_budget: device bytes that requests in flight may hold (outputs plus
@@ -180,14 +192,38 @@ VC_API vcg_server *vcg_server_create(vc_archive *a, uint64_t device_budget, uint
     s->cap = 1024;
     s->reqs = (srv_req *)calloc(s->cap, sizeof(srv_req));
     if (!s->reqs) { free(s); return NULL; }
+    for (int i = 0; i < workers; ++i) {
+        struct srv_worker *w = &s->w[i];
+        w->s = s;
+        w->batch = (vcg_region_request *)malloc(max_batch * sizeof(vcg_region_request));
+        w->st = (vc_status *)malloc(max_batch * sizeof(vc_status));
+        w->tix = (uint64_t *)malloc(max_batch * sizeof(uint64_t));
+        if (!w->batch || !w->st || !w->tix) {
+            free_workers(s);
+            free(s->reqs);
+            free(s);
+            return NULL;
+        }
+    }
     pthread_mutex_init(&s->mu, NULL);
     pthread_cond_init(&s->work_cv, NULL);
     pthread_cond_init(&s->done_cv, NULL);
+    // the workers start once they are all created (they read nworkers under mu)
+    pthread_mutex_lock(&s->mu);
     for (int i = 0; i < workers; ++i) {
-        if (pthread_create(&s->th[i], NULL, worker, s) != 0) break;
+        if (pthread_create(&s->th[i], NULL, worker, &s->w[i]) != 0) break;
         s->nworkers++;
     }
-    if (!s->nworkers) { free(s->reqs); free(s); return NULL; }
+    pthread_mutex_unlock(&s->mu);
+    if (!s->nworkers) {
+        pthread_mutex_destroy(&s->mu);
+        pthread_cond_destroy(&s->work_cv);
+        pthread_cond_destroy(&s->done_cv);
+        free_workers(s);
+        free(s->reqs);
+        free(s);
+        return NULL;
+    }
     return s;
 }
 
@@ -265,6 +301,7 @@ VC_API void vcg_server_destroy(vcg_server *s) {
     pthread_mutex_destroy(&s->mu);
     pthread_cond_destroy(&s->work_cv);
     pthread_cond_destroy(&s->done_cv);
+    free_workers(s);
     free(s->reqs);
     free(s);
 }
