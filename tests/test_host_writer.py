@@ -112,3 +112,43 @@ def test_random_sessions(vc, host_writer, ref_writer):
         assert W.run(host_writer, s, vc.synth, async_atoms=True)[-1] == want[-1], (trial, s)
         appended += sum(1 for o, r in zip(s["ops"], want) if o[0] in ("atom", "box") and r == 0)
     assert appended > 30
+
+
+def build_mt(tmp, oracle, tsan=False):
+    exe = str(tmp / ("host_writer_mt_tsan" if tsan else "host_writer_mt"))
+    csrc = os.path.join(ROOT, "volume-compressor_gb300", "csrc")
+    odir = os.path.join(ROOT, "oracle")
+    flags = ["-O1", "-g", "-fsanitize=thread"] if tsan else ["-O2"]
+    r = subprocess.run(["gcc", *flags, "-std=gnu11", "-I", os.path.join(ROOT, "include"), "-I", csrc, "-I", odir,
+                        os.path.join(ROOT, "tests", "host_writer_mt.c"), os.path.join(ROOT, "tests", "host_writer.c"),
+                        os.path.join(csrc, "vc_writer.c"), os.path.join(csrc, "vc_host.c"), "-L", odir, "-loracle",
+                        "-Wl,-rpath," + odir, "-lpthread", "-lm", "-o", exe], capture_output=True, text=True)
+    return exe, r
+
+
+def test_concurrent_appends(oracle, tmp_path):
+    """Threads (1, 4 and 16) append every atom of two LODs of a volume spanning
+    three regions, in shuffled orders, synchronously, queued and as zero marks,
+    with coverage queries between: every atom of the closed file has the
+    coverage it was given and decodes (oracle's reader) to what the oracle's
+    own encode and decode of its source give (tests/host_writer_mt.c)."""
+    exe, r = build_mt(tmp_path, oracle)
+    assert r.returncode == 0, r.stderr[-2000:]
+    for threads in (1, 4, 16):
+        r = subprocess.run([exe, str(tmp_path / f"mt{threads}.vca"), str(threads)], capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0 and r.stdout.strip() == "atoms 462 wrong 0" and not r.stderr, (threads, r.stdout,
+                                                                                                 r.stderr[-2000:])
+
+
+def test_concurrent_appends_race_free(oracle, tmp_path):
+    """The same with 8 threads under ThreadSanitizer: no data race in the
+    writer's batching, index, slot and cursor updates."""
+    exe, r = build_mt(tmp_path, oracle, tsan=True)
+    if r.returncode:
+        pytest.skip("no ThreadSanitizer with this compiler: " + r.stderr[-200:])
+    r = subprocess.run([exe, str(tmp_path / "mt.vca"), "8"], capture_output=True, text=True, timeout=900)
+    if "FATAL: ThreadSanitizer" in r.stderr:
+        pytest.skip(r.stderr.strip().splitlines()[0])
+    assert "WARNING: ThreadSanitizer" not in r.stderr, r.stderr[:4000]
+    assert r.returncode == 0 and r.stdout.strip() == "atoms 462 wrong 0", r.stdout + r.stderr[-2000:]
