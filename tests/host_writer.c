@@ -7,6 +7,7 @@
 // the vc.h writer API, so that writer sessions run on it as on the reference's
 // writer: the file layout, the region index, the slot blocks, the zero marks,
 // the coverage reads and the close are this library's own host code.
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -15,9 +16,15 @@
 #include "vc_internal.h"
 #include "vc_oracle.h"
 
-// ---- the stand-in encoder: vcd_encode_segments (vc_internal.h) on the host
+// ---- the stand-in encoder: vcd_encode_segments (vc_internal.h) on the host.
+// Each thread's payload buffer lives until the thread ends (as the device
+// layer's per-thread buffer does).
 static __thread uint8_t *g_pay;
 static __thread uint64_t g_pay_cap;
+static pthread_key_t g_pay_key;
+static pthread_once_t g_pay_once = PTHREAD_ONCE_INIT;
+static void pay_free(void *p) { free(p); }
+static void pay_key(void) { pthread_key_create(&g_pay_key, pay_free); }
 
 int vcd_encode_segments(const vcd_seg *segs, int nseg, const float *qs, int nq, uint8_t **pay, uint64_t *pay_bytes) {
     (void)nq;
@@ -44,8 +51,10 @@ int vcd_encode_segments(const vcd_seg *segs, int nseg, const float *qs, int nq, 
                         if (!p) return VC_ERR_OOM;
                         g_pay = p;
                         g_pay_cap = cap;
+                        pthread_once(&g_pay_once, pay_key);
+                        pthread_setspecific(g_pay_key, p);
                     }
-                    memcpy(g_pay + used, out, len);
+                    if (len) memcpy(g_pay + used, out, len);
                     S->len[i] = len;
                     S->off[i] = used;
                     used += len;

@@ -114,11 +114,11 @@ def test_random_sessions(vc, host_writer, ref_writer):
     assert appended > 30
 
 
-def build_mt(tmp, oracle, tsan=False):
-    exe = str(tmp / ("host_writer_mt_tsan" if tsan else "host_writer_mt"))
+def build_mt(tmp, oracle, sanitize=None):
+    exe = str(tmp / ("host_writer_mt_" + (sanitize or "plain").replace(",", "_")))
     csrc = os.path.join(ROOT, "volume-compressor_gb300", "csrc")
     odir = os.path.join(ROOT, "oracle")
-    flags = ["-O1", "-g", "-fsanitize=thread"] if tsan else ["-O2"]
+    flags = ["-O1", "-g", "-fno-omit-frame-pointer", "-fsanitize=" + sanitize] if sanitize else ["-O2"]
     r = subprocess.run(["gcc", *flags, "-std=gnu11", "-I", os.path.join(ROOT, "include"), "-I", csrc, "-I", odir,
                         os.path.join(ROOT, "tests", "host_writer_mt.c"), os.path.join(ROOT, "tests", "host_writer.c"),
                         os.path.join(csrc, "vc_writer.c"), os.path.join(csrc, "vc_host.c"), "-L", odir, "-loracle",
@@ -144,11 +144,23 @@ def test_concurrent_appends(oracle, tmp_path):
 def test_concurrent_appends_race_free(oracle, tmp_path):
     """The same with 8 threads under ThreadSanitizer: no data race in the
     writer's batching, index, slot and cursor updates."""
-    exe, r = build_mt(tmp_path, oracle, tsan=True)
+    exe, r = build_mt(tmp_path, oracle, "thread")
     if r.returncode:
         pytest.skip("no ThreadSanitizer with this compiler: " + r.stderr[-200:])
     r = subprocess.run([exe, str(tmp_path / "mt.vca"), "8"], capture_output=True, text=True, timeout=900)
     if "FATAL: ThreadSanitizer" in r.stderr:
         pytest.skip(r.stderr.strip().splitlines()[0])
     assert "WARNING: ThreadSanitizer" not in r.stderr, r.stderr[:4000]
+    assert r.returncode == 0 and r.stdout.strip() == "atoms 462 wrong 0", r.stdout + r.stderr[-2000:]
+
+
+def test_concurrent_appends_memory_clean(oracle, tmp_path):
+    """The same with 8 threads under AddressSanitizer and UBSan: no invalid
+    access, no undefined behaviour and nothing leaked at exit."""
+    exe, r = build_mt(tmp_path, oracle, "address,undefined")
+    if r.returncode:
+        pytest.skip("no AddressSanitizer with this compiler: " + r.stderr[-200:])
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1", UBSAN_OPTIONS="print_stacktrace=1")
+    r = subprocess.run([exe, str(tmp_path / "mt.vca"), "8"], capture_output=True, text=True, timeout=900, env=env)
+    assert "runtime error" not in r.stderr and "ERROR: " not in r.stderr, r.stderr[:4000]
     assert r.returncode == 0 and r.stdout.strip() == "atoms 462 wrong 0", r.stdout + r.stderr[-2000:]
