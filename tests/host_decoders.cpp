@@ -84,8 +84,9 @@ int main(int argc, char **argv) {
     if (!f) return 2;
     uint32_t n = 0;
     if (fread(&n, 4, 1, f) != 1) return 2;
-    uint32_t bs[9];
+    uint32_t bs[10];   // the band table and a copy of its end, as the kernels hold it for RcLane
     band_table(bs);
+    bs[9] = bs[8];
     const char *names[5] = {"latency", "staged", "scalar", "lockstep", "per-lane"};
     int diff[5] = {0, 0, 0, 0, 0};
     for (uint32_t k = 0; k < n; ++k) {

@@ -76,8 +76,9 @@ int main(int argc, char **argv) {
         if (fread(h, 4, 2, f) != 2) return 2;
         const uint32_t nent = h[0], nbytes = h[1];
         // entries 16-byte aligned with room for the encoder's look-ahead loads
-        uint32_t *ent = (uint32_t *)aligned_alloc(16, 4 * ((size_t)nent + 16) + 64);
-        memset(ent, 0, 4 * ((size_t)nent + 16) + 64);
+        const size_t ebytes = (4 * ((size_t)nent + 16) + 64 + 15) & ~(size_t)15;   // a multiple of the alignment
+        uint32_t *ent = (uint32_t *)aligned_alloc(16, ebytes);
+        memset(ent, 0, ebytes);
         std::vector<uint8_t> want(nbytes + 1);
         if (nent && fread(ent, 4, nent, f) != nent) return 2;
         if (nbytes && fread(want.data(), 1, nbytes, f) != nbytes) return 2;

@@ -141,9 +141,9 @@ __global__ void k_ua_scatter(BatchJob J) {
 constexpr int kBatchLaneThreads = 64;
 
 __global__ void __launch_bounds__(kBatchLaneThreads) k_rc_batch_lanes(BatchJob J) {
-    __shared__ uint32_t bstart[9];
+    __shared__ uint32_t bstart[10];   // the band table and a copy of its end (RcLane)
     __shared__ uint32_t S[12 * kBatchLaneThreads];
-    if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
+    if (threadIdx.x < 10) bstart[threadIdx.x] = J.band_start[threadIdx.x < 9 ? threadIdx.x : 8];
     __syncthreads();
     const uint32_t n_present = J.sort_ctl[kSortBuckets];   // 0 when the scalar kernel decodes this batch
     if ((uint64_t)blockIdx.x * kBatchLaneThreads >= n_present) return;   // whole CTA idle

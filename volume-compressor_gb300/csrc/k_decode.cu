@@ -244,9 +244,9 @@ constexpr int kLaneThreads = 64;   // 2 warps per CTA
 constexpr int kLaneUnroll = 8;     // steps between warp votes
 
 __global__ void __launch_bounds__(kLaneThreads) k_rc_lanes(DecodeJob J) {
-    __shared__ uint32_t bstart[9];
+    __shared__ uint32_t bstart[10];   // the band table and a copy of its end (RcLane)
     __shared__ uint32_t S[12 * kLaneThreads];   // magnitude contexts, lane-interleaved
-    if (threadIdx.x < 9) bstart[threadIdx.x] = J.band_start[threadIdx.x];
+    if (threadIdx.x < 10) bstart[threadIdx.x] = J.band_start[threadIdx.x < 9 ? threadIdx.x : 8];
     __syncthreads();
     const uint64_t i = (uint64_t)blockIdx.x * kLaneThreads + threadIdx.x;
     const bool active = i < J.sort_ctl[kSortBuckets];
@@ -445,14 +445,14 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
 __global__ void __launch_bounds__(kFusedThreads, 1) k_decode_fused(DecodeJob J, uint32_t *queue, uint32_t per,
                                                                     uint32_t *fail) {
     extern __shared__ int32_t T[];   // transform tile
-    __shared__ uint32_t bstart[9];
+    __shared__ uint32_t bstart[10];   // the band table and a copy of its end (RcLane)
     __shared__ uint32_t S[12 * kFusedRcThreads];
     __shared__ int32_t dqs[VCD_NCLASS], dqb[VCD_NCLASS];
     __shared__ uint32_t alt[1024];
     __shared__ uint32_t q_tail;   // slots of this CTA's queue handed out
     __shared__ uint32_t cur[2];   // atom of the transform's current iteration (double-buffered)
     const int tid = threadIdx.x;
-    if (tid < 9) bstart[tid] = J.band_start[tid];
+    if (tid < 10) bstart[tid] = J.band_start[tid < 9 ? tid : 8];
     for (int i = tid; i < VCD_NCLASS; i += kFusedThreads) { dqs[i] = J.dq->step[i]; dqb[i] = J.dq->bias[i]; }
     for (int i = tid; i < 1024; i += kFusedThreads) alt[i] = J.alt_mask[i];
     if (tid == 0) q_tail = 0;

@@ -327,6 +327,8 @@ struct RcLane {
     uint32_t *dst;         // coefficient list (scan position | level << 16)
     uint32_t n, cap, bad;  // entries decoded (all, also past cap); list capacity; malformed
 
+    // bstart: the 9-entry band table followed by a copy of its last entry (a
+    // lane that ends at the last band's end loads the entry after it).
     // S: this lane's 12 magnitude contexts at S[0], S[st], ..., S[11 * st]
     __device__ __forceinline__ void init(const uint8_t *s, uint32_t l, bool active, const uint32_t *bstart,
                                          uint32_t *S, uint32_t st, uint32_t *d, uint32_t cp) {
