@@ -44,12 +44,20 @@ def atom_streams(oracle, data):
     return out
 
 
-@pytest.fixture(scope="module")
-def harness(tmp_path_factory):
-    exe = str(tmp_path_factory.mktemp("host_decoders") / "host_decoders")
+SANITIZE = ["-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer", "-fno-sanitize-recover=undefined"]
+
+
+def build(tmp_path_factory, flags, name):
+    exe = str(tmp_path_factory.mktemp(name) / name)
     src = os.path.join(ROOT, "tests", "host_decoders.cpp")
     inc = os.path.join(ROOT, "volume-compressor_gb300", "csrc")
-    r = subprocess.run(["g++", "-O2", "-std=c++17", "-w", "-I", inc, src, "-o", exe], capture_output=True, text=True)
+    r = subprocess.run(["g++", *flags, "-std=c++17", "-w", "-I", inc, src, "-o", exe], capture_output=True, text=True)
+    return exe, r
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    exe, r = build(tmp_path_factory, ["-O2"], "host_decoders")
     if r.returncode:
         pytest.fail(r.stderr[-2000:])
     return exe
@@ -70,17 +78,22 @@ def run(harness, oracle, streams, tmp_path):
     return {name: int(diff) for name, diff, _ in rows}
 
 
-def test_golden_archive_streams(harness, oracle, golden, tmp_path):
+def golden_streams(oracle, golden):
     streams = []
     for name in ("synth_64_t10", "synth_prime_97x131x65_t20", "synth_flat_96x64x33_t100", "ref_test_basic",
                  "extreme_sat", "extreme_line", "extreme_voxel", "tiny_1x1x1"):
         streams += atom_streams(oracle, load_archive(golden[name]))
+    return streams
+
+
+def test_golden_archive_streams(harness, oracle, golden, tmp_path):
+    streams = golden_streams(oracle, golden)
     assert len(streams) > 300
     assert run(harness, oracle, streams, tmp_path) == dict.fromkeys(
         ("latency", "staged", "scalar", "lockstep", "per-lane"), 0)
 
 
-def test_noise_escapes_truncation_and_random_streams(harness, oracle, tmp_path):
+def other_streams(oracle):
     rng = np.random.default_rng(0xDEC0DE)
     vol = rng.integers(0, 256, (64, 64, 64)).astype(np.uint8)
     s, data = oracle.encode_fixed_q(vol, 1.0, [0.05] * 8)   # the largest levels: many escapes
@@ -95,7 +108,23 @@ def test_noise_escapes_truncation_and_random_streams(harness, oracle, tmp_path):
             streams.append(rng.integers(0, 256, n).astype(np.uint8).tobytes())
     for ones in (31, 32, 33, 40):   # escape prefixes at and past the limit
         streams.append(hostile_payload(prefix_ones=ones)[1:])
+    return streams
+
+
+def test_noise_escapes_truncation_and_random_streams(harness, oracle, tmp_path):
+    streams = other_streams(oracle)
     bad = [expected(oracle, s)[0] for s in streams]
     assert sum(bad) >= 2 and sum(bad) < len(streams)
     assert run(harness, oracle, streams, tmp_path) == dict.fromkeys(
+        ("latency", "staged", "scalar", "lockstep", "per-lane"), 0)
+
+
+def test_all_streams_under_sanitizers(oracle, golden, tmp_path_factory, tmp_path):
+    """Both stream sets through a build with AddressSanitizer and UBSan: no
+    out-of-bounds access and no undefined behaviour in any decoder (this found
+    the per-lane decoder reading one entry past the band table)."""
+    exe, r = build(tmp_path_factory, SANITIZE, "host_decoders_san")
+    if r.returncode:
+        pytest.skip("no AddressSanitizer / UBSan with this compiler: " + r.stderr[-200:])
+    assert run(exe, oracle, golden_streams(oracle, golden) + other_streams(oracle), tmp_path) == dict.fromkeys(
         ("latency", "staged", "scalar", "lockstep", "per-lane"), 0)

@@ -21,14 +21,27 @@ IDX = np.arange(32768)
 SCAN = np.lexsort((IDX, (IDX >> 10) + ((IDX >> 5) & 31) + (IDX & 31)))
 
 
-@pytest.fixture(scope="module")
-def harness(tmp_path_factory):
-    exe = str(tmp_path_factory.mktemp("host_encoder") / "host_encoder")
+def build(tmp_path_factory, flags, name):
+    exe = str(tmp_path_factory.mktemp(name) / name)
     src = os.path.join(ROOT, "tests", "host_encoder.cpp")
     inc = os.path.join(ROOT, "volume-compressor_gb300", "csrc")
-    r = subprocess.run(["g++", "-O2", "-std=c++17", "-w", "-I", inc, src, "-o", exe], capture_output=True, text=True)
+    r = subprocess.run(["g++", *flags, "-std=c++17", "-w", "-I", inc, src, "-o", exe], capture_output=True, text=True)
+    return exe, r
+
+
+@pytest.fixture(scope="module", params=["plain", "sanitized"])
+def harness(tmp_path_factory, request):
+    """The plain build, and one with AddressSanitizer and UBSan (no
+    out-of-bounds access or undefined behaviour may show up)."""
+    if request.param == "plain":
+        exe, r = build(tmp_path_factory, ["-O2"], "host_encoder")
+        if r.returncode:
+            pytest.fail(r.stderr[-2000:])
+        return exe
+    exe, r = build(tmp_path_factory, ["-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer",
+                                      "-fno-sanitize-recover=undefined"], "host_encoder_san")
     if r.returncode:
-        pytest.fail(r.stderr[-2000:])
+        pytest.skip("no AddressSanitizer / UBSan with this compiler: " + r.stderr[-200:])
     return exe
 
 
